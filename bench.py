@@ -1,0 +1,349 @@
+"""Benchmark of the GB300 Euler step (cell-updates/s).
+
+Workload (default): 2D radial Sod, 1024 x 1024 cells on [-1,1]^2, rho=p=1 for
+r<0.5 and rho=0.125, p=0.1 outside, zero velocity, transmissive borders,
+CFL 0.5, integrated towards t=0.25 (a step = one SSP-RK3 step of the whole
+mesh; when a run reaches t=0.25 the state restarts from the initial state,
+outside the timed region).  Synthetic input: the initial state is generated
+from the problem definition, no dataset is involved.
+
+value  : cell-updates/s with the state resident in HBM; each step is timed with
+         CUDA events on the library stream, and L2 is flushed (a 512 MB write)
+         between timed steps, outside the events.
+e2e    : the same metric through the public C ABI with host buffers:
+         upload of the AoS state from pinned memory, one step, download.
+roofline / fp64: the stage-2 kernel (dominant, 120 B/cell algorithmic) timed
+         per launch with events; peaks from MEASURED_PEAKS.json.
+cpu_baseline: the oracle (C restatement, bit-identical to the reference
+         sources) on the host cores, on a bounded sample of steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CELL_BYTES_STEP = 320          # algorithmic HBM bytes per cell-update (8 x 5 fields x 8 B)
+STAGE_BYTES = {1: 80, 2: 120, 3: 120}
+FP64_OPS_PER_CELL_STAGE = None  # filled from the kernel model below (fast arithmetic, 2D)
+
+
+def fp64_ops_per_cell_update_2d():
+    """FP64 instructions per cell-update of the fast 2D kernel (per-cell model):
+    record: 1/rho (division, ~9 DFMA-equivalent), 3 mul (u,v,w), 2 fma + 1 mul (rho|u|^2),
+    2 (p), 2 + sqrt (~10) (a), 1 (E+p), fluxes 2 dirs x 5, 1 shared mul  -> ~41
+    faces: 2 per cell x (5 x (add, sub, fma) + max) = 32; accumulate 5 x 3 = 15;
+    stage update ~(5 stage1: 0, stage2: 5 fma load + 15, stage3: 15)/3 avg ~ 12."""
+    return 3 * (41 + 32 + 15) + 35
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic():
+    p = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 ".bench_clocks_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_sample_worker(args):
+    """One process: oracle steps of the workload, bounded by wall time."""
+    n, steps_cap, seconds = args
+    import oracle
+    import minimmerflow_gb300.problem as P
+    case = P.radial_sod_2d(n=n)
+    m = oracle.OracleMesh(case.problem, 2, case.n, case.origin, case.length)
+    U = m.initial_state(oracle.params(sod_radius=0.5))
+    lib = oracle.lib()
+    done, t0 = 0, lib.orc_now()
+    while done < steps_cap:
+        U, t, s = m.run(U, case.cfl, t_end=case.t_end, max_steps=1)
+        done += 1
+        if lib.orc_now() - t0 > seconds:
+            break
+    return done * case.ncells, lib.orc_now() - t0
+
+
+def cpu_baseline(n, seconds, procs):
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    if procs <= 1:
+        cells, secs = cpu_sample_worker((n, 10 ** 6, seconds))
+        total = cells / secs
+        sample = "%d steps of the %dx%d radial Sod on 1 core (%.1f s)" % (cells // (n * n), n, n, secs)
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(procs) as pool:
+            res = pool.map(cpu_sample_worker, [(n, 10 ** 6, seconds)] * procs)
+        total = sum(c / s for c, s in res)
+        sample = ("%d independent replicas of the %dx%d radial Sod, one per core, %d steps each (~%.0f s)"
+                  % (procs, n, n, res[0][0] // (n * n), res[0][1]))
+    return {"value": total, "unit": "cell-updates/s", "cores": procs, "kind": "port", "sample": sample}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args, world, rank, local, dist):
+    import numpy as np
+    import torch
+    import minimmerflow_gb300 as mmf
+
+    torch.cuda.set_device(local)
+    case = mmf.problem.radial_sod_2d(n=args.n)
+    U0 = case.initial_state()
+    ncell = case.ncells
+    s = case.solver(arith=args.arith, device=local, chunk=args.chunk)
+    stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def restart():
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, case.t_end, -1)
+
+    restart()
+    steps_done = 0
+
+    def ensure_room():
+        nonlocal steps_done
+        t, st = s.time_info()
+        if t >= case.t_end - 1e-15:
+            restart()
+
+    # warm-up
+    for _ in range(args.warmup):
+        ensure_room()
+        s.advance_async(1)
+    s.synchronize()
+
+    def timed_steps(k):
+        """k steps, each bracketed by events on the library stream; L2 flushed between."""
+        durs = []
+        check_every = 16
+        for i in range(k):
+            if i % check_every == 0:
+                ensure_room()
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.advance_async(1)
+            e1.record(stream)
+            e1.synchronize()
+            durs.append(e0.elapsed_time(e1) / 1e3)
+        return durs
+
+    # the run must not cross t_end inside the timed region: check room per 16 steps
+    launches0 = s.launch_count
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    durs = timed_steps(args.steps)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    launches = s.launch_count - launches0
+    total = sum(durs)
+    if dist is not None:
+        tt = torch.tensor([total], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total = float(tt.item())
+    value = world * ncell * args.steps / total
+
+    # per-stage launch times (stage 2 = dominant kernel, roofline)
+    stage_t = {1: [], 2: [], 3: []}
+    for i in range(max(8, min(args.steps, 64))):
+        if i % 16 == 0:
+            ensure_room()
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        for st in (1, 2, 3):
+            s.rk_stage(st)
+            ev[st].record(stream)
+        ev[3].synchronize()
+        for st in (1, 2, 3):
+            stage_t[st].append(ev[st - 1].elapsed_time(ev[st]) / 1e3)
+    st_mean = {k: statistics.mean(v) for k, v in stage_t.items()}
+    dominant = max(st_mean, key=st_mean.get)
+
+    # e2e through the C ABI with pinned host buffers
+    host = torch.empty((ncell, 5), dtype=torch.float64, pin_memory=True)
+    hv = host.numpy()
+    hv[:] = U0
+    s.time_setup(case.cfl, 0.0, case.t_end, -1)
+    k_e2e = max(3, min(args.steps, 50))
+    for _ in range(2):
+        s.advance_host(hv, 1)
+    hv[:] = U0
+    s.time_setup(case.cfl, 0.0, case.t_end, -1)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        s.advance_host(hv, 1)
+    e2e_s = time.perf_counter() - t0
+    e2e_val = world * ncell * k_e2e / e2e_s
+    s.close()
+    return dict(value=value, total=total, clocks=clocks, launches=launches, st_mean=st_mean, dominant=dominant,
+                e2e=e2e_val, ncell=ncell, case=case)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-procs", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup(args)
+    workload = {"workload": "2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, to t=0.25, order 1, FP64" % (args.n, args.n),
+                "cells": args.n * args.n, "l2": "flushed between timed steps (512 MB write)",
+                "parallelism": "replicas x%d" % world}
+    metric = "cell-updates/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        procs = args.cpu_procs or os.cpu_count() or 1
+        # each 'step' of the reference arm is a bounded sample of the workload
+        per = max(2.0, min(args.cpu_seconds, 60.0 / max(1, args.steps + args.warmup)))
+        base = cpu_baseline(args.n, per * max(1, args.steps), procs)
+        line = {"metric": metric, "value": base["value"], "unit": metric, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * args.n * args.n / base["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": workload, "impl": "reference",
+                "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    r = run_ours(args, world, rank, local, dist)
+    if rank != 0:
+        return
+    hbm_peak, peak_src = read_peaks()
+    ncell = r["ncell"]
+    dom = r["dominant"]
+    achieved = STAGE_BYTES[dom] * ncell / r["st_mean"][dom] / 1e9
+    traffic_rec = read_traffic()
+    traffic = None
+    if traffic_rec and str(args.n) in traffic_rec.get("per_launch_bytes", {}):
+        traffic = traffic_rec["per_launch_bytes"][str(args.n)].get("stage%d" % dom)
+    fp64_ops = fp64_ops_per_cell_update_2d()
+    fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock)
+    line = {
+        "metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload,
+        "arith": args.arith,
+        "roofline": {"bound": "hbm", "kernel": "stage%d (stage2d_kernel<%s>)" % (dom, args.arith),
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": STAGE_BYTES[dom] * ncell,
+                     "stage_ms": {str(k): 1e3 * v for k, v in r["st_mean"].items()}},
+        "fp64": {"ops_per_cell_update_model": fp64_ops,
+                 "achieved_ops_per_s": fp64_ops * r["value"] / world,
+                 "peak_ops_per_s": fp64_peak, "frac": fp64_ops * r["value"] / world / fp64_peak,
+                 "peak_source": "measured DFMA issue rate (probe), not in MEASURED_PEAKS.json"},
+        "clocks": r["clocks"],
+        "gpu_launches": r["launches"],
+        "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,
+                "d2h_bytes_per_step": 40 * ncell},
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * mmf_gb300.h -- C ABI of the GB300 (sm_103a) finite-volume Euler step that
+ * replaces the hot path of optimad/minimmerflow: face reconstruction
+ * (src/reconstruction.cpp), interface fluxes and residual accumulation
+ * (src/euler.cpp), the SSP-RK3 stage update and the CFL time step (inline in
+ * src/main.cpp:377-506).
+ *
+ * Conventions (mirroring the reference boundary, src/euler.hpp:37-48):
+ *  - The caller owns every host buffer; the library writes results into
+ *    caller storage and never calls exit().
+ *  - Cell state crosses the ABI as the reference's PiercedStorage raw layout:
+ *    AoS double[n_raw][5] in raw-id order, fields (rho, rho u, rho v, rho w,
+ *    rho E) = FID_RHO..FID_RHO_E (src/constants.hpp:43-47).  A raw-id -> grid
+ *    cell map (mmf_set_cell_map) lets it follow bitpit's octree (Morton) order.
+ *  - Every function returns an int status: MMF_OK (0) or a negative code;
+ *    mmf_last_error() describes the last failure of the calling thread.
+ *  - One context = one GPU, one CUDA stream; calls on a context are ordered
+ *    and not thread-safe (the reference is single-threaded per rank).
+ *  - No CPU fallback: without a usable CUDA device mmf_create fails.
+ */
+#ifndef MMF_GB300_H
+#define MMF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMF_ABI_VERSION 1
+
+/* status codes */
+#define MMF_OK 0
+#define MMF_ERR_ARG (-1)          /* invalid argument */
+#define MMF_ERR_CUDA (-2)         /* CUDA runtime error (no device, launch failure, ...) */
+#define MMF_ERR_STATE (-3)        /* non-physical state seen (rho < 0, p < 0, NaN) */
+#define MMF_ERR_UNSUPPORTED (-4)  /* unsupported order / configuration */
+#define MMF_ERR_NOMEM (-5)        /* device allocation failed */
+
+/* border conditions: src/constants.hpp:58-62; MMF_BC_PERIODIC has no
+ * reference counterpart (periodic wrap of the two opposite borders). */
+#define MMF_BC_NONE (-1)
+#define MMF_BC_FREE_FLOW 0
+#define MMF_BC_REFLECTING 1
+#define MMF_BC_WALL 2
+#define MMF_BC_DIRICHLET 3
+#define MMF_BC_PERIODIC 16
+
+/* arithmetic of the fused step */
+#define MMF_ARITH_REFERENCE 0   /* reference operation order, bit-identical results */
+#define MMF_ARITH_FAST 1        /* one division + one sqrt per cell, FMA; round-off level agreement */
+
+/* status bits reported by mmf_get_status (src/euler.cpp:93-101 logs the first two) */
+#define MMF_STATUS_NEG_DENSITY 1u
+#define MMF_STATUS_NEG_PRESSURE 2u
+#define MMF_STATUS_NAN 4u
+
+typedef struct mmf_ctx mmf_ctx;
+
+/* Uniform Cartesian mesh, the mesh VolOctree builds with uniform refinement
+ * (src/main.cpp:146-155).  Cell (i,j,k) has centroid origin + (i+1/2, j+1/2,
+ * k+1/2) h, volume h^dim, faces of area h^(dim-1). */
+typedef struct {
+    int dim;                   /* 2 or 3 */
+    int n[3];                  /* cells per direction (n[2] = 1 in 2D) */
+    double origin[3];
+    double h;                  /* cell edge = minCellSize (src/main.cpp:351-356) */
+    int bc_lo[3], bc_hi[3];    /* border condition per side (MMF_BC_*) */
+    double dirichlet_prim[5];  /* (p,u,v,w,T) behind MMF_BC_DIRICHLET borders (src/problem.cpp:458-468) */
+    int order;                 /* reconstruction order: 1 (src/reconstruction.cpp:67-79) */
+    int arith;                 /* MMF_ARITH_* */
+    int chunk;                 /* marching chunk (rows 2D / planes 3D); 0 = default */
+} mmf_grid;
+
+/* ---- context --------------------------------------------------------- */
+int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out);
+int mmf_destroy(mmf_ctx *ctx);
+const char *mmf_last_error(void);
+int mmf_abi_version(void);
+/* Number of kernel launches issued by this context since creation. */
+int64_t mmf_launch_count(const mmf_ctx *ctx);
+
+/* Raw-id -> grid-cell map (grid index = i + n0 (j + n1 k)); n_raw must equal
+ * the cell count.  Default: identity (row-major raw order).  Replaces the
+ * id -> raw-position lookups of src/euler.cpp:158-178. */
+int mmf_set_cell_map(mmf_ctx *ctx, int64_t n_raw, const int64_t *raw_to_cell);
+
+/* ---- state transfer (PiercedStorage AoS raw layout <-> device SoA) --- */
+int mmf_upload_state(mmf_ctx *ctx, const double *aos, int64_t n_raw);
+int mmf_download_state(mmf_ctx *ctx, double *aos, int64_t n_raw);
+/* Same with device pointers (AoS [n_raw][5] already in device memory). */
+int mmf_upload_state_device(mmf_ctx *ctx, const double *d_aos, int64_t n_raw);
+int mmf_download_state_device(mmf_ctx *ctx, double *d_aos, int64_t n_raw);
+
+/* ---- reference entry points ------------------------------------------ */
+/* euler::computeRHS (src/euler.hpp:41-43): residual of every cell (not
+ * divided by the volume) and the maximum face eigenvalue, for the state
+ * 'cons' (host AoS raw layout).  Always uses the reference arithmetic. */
+int mmf_compute_rhs(mmf_ctx *ctx, const double *cons, double *rhs, double *max_eig, int64_t n_raw);
+/* reconstruction::computePolynomials (src/reconstruction.hpp:41-42) on the
+ * uploaded state: a no-op at order 1. */
+int mmf_compute_polynomials(mmf_ctx *ctx);
+
+/* ---- time loop (src/main.cpp:377-506) on the uploaded state ----------- */
+/* Sets t, t_end (INFINITY allowed with max_steps >= 0), CFL; minCellSize = h. */
+int mmf_time_setup(mmf_ctx *ctx, double cfl, double t, double t_end, int64_t max_steps);
+/* Runs up to n_steps SSP-RK3 steps (stopping at t_end / max_steps), device
+ * resident, replayed from a CUDA graph; returns the time and steps done. */
+int mmf_advance(mmf_ctx *ctx, int64_t n_steps, double *t_out, int64_t *steps_done);
+/* Enqueues n_steps graph-replayed steps without waiting (no host sync); the
+ * time and step count are read later with mmf_time_info. */
+int mmf_advance_async(mmf_ctx *ctx, int64_t n_steps);
+/* Current time and steps done since mmf_time_setup (synchronises). */
+int mmf_time_info(mmf_ctx *ctx, double *t, int64_t *step);
+/* The CUDA stream (cudaStream_t) all work of this context is ordered on. */
+void *mmf_get_stream(mmf_ctx *ctx);
+/* Host-buffer form: uploads 'aos', advances n_steps, downloads into 'aos'. */
+int mmf_advance_host(mmf_ctx *ctx, double *aos, int64_t n_raw, int64_t n_steps, double *t_out);
+/* Last step's dt and stage-1 maxEig (the reference logs both, main.cpp:399). */
+int mmf_last_step_info(mmf_ctx *ctx, double *dt, double *max_eig);
+/* Status bits accumulated since the last call (cleared on read). */
+int mmf_get_status(mmf_ctx *ctx, unsigned *status);
+/* Blocks until queued work is done. */
+int mmf_synchronize(mmf_ctx *ctx);
+
+/* Single stages, for drivers that keep the reference loop structure:
+ * stage 1 = computeRHS(U) + maxEig; 2 = W update (needs dt); 3 = close. */
+int mmf_rk_stage(mmf_ctx *ctx, int stage);
+
+/* ---- unit-level functions, batched over n items (host AoS buffers) ---- */
+/* utils::conservative2primitive / primitive2conservative (src/utils.hpp:34-35) */
+int mmf_cons2prim(int64_t n, const double *cons, double *prim);
+int mmf_prim2cons(int64_t n, const double *prim, double *cons);
+/* euler::evalFluxes (src/euler.hpp:39): cons[n][5], prim[n][5], normal[n][3] */
+int mmf_eval_fluxes(int64_t n, const double *cons, const double *prim, const double *normal, double *flux);
+/* euler::evalSplitting (src/euler.hpp:37) */
+int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, const double *normal,
+                       double *flux, double *lambda);
+/* euler::evalInterfaceBCValues (src/euler.hpp:45-48); dirichlet_prim may be NULL */
+int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
+                       const double *dirichlet_prim, double *cons_bc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

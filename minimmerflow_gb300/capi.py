@@ -1,0 +1,96 @@
+"""ctypes binding of the C ABI declared in include/mmf_gb300.h.
+
+Loading fails loudly when the CUDA library is missing: there is no CPU
+fallback behind these functions.
+"""
+import ctypes as C
+import os
+
+from . import _build
+
+MMF_OK = 0
+MMF_ERR_ARG, MMF_ERR_CUDA, MMF_ERR_STATE, MMF_ERR_UNSUPPORTED, MMF_ERR_NOMEM = -1, -2, -3, -4, -5
+BC_NONE, BC_FREE_FLOW, BC_REFLECTING, BC_WALL, BC_DIRICHLET, BC_PERIODIC = -1, 0, 1, 2, 3, 16
+ARITH_REFERENCE, ARITH_FAST = 0, 1
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTS = [
+    "mmf_create", "mmf_destroy", "mmf_last_error", "mmf_abi_version", "mmf_launch_count",
+    "mmf_set_cell_map", "mmf_upload_state", "mmf_download_state", "mmf_upload_state_device",
+    "mmf_download_state_device", "mmf_compute_rhs", "mmf_compute_polynomials", "mmf_time_setup",
+    "mmf_advance", "mmf_advance_async", "mmf_time_info", "mmf_get_stream", "mmf_advance_host", "mmf_last_step_info", "mmf_get_status", "mmf_synchronize",
+    "mmf_rk_stage", "mmf_cons2prim", "mmf_prim2cons", "mmf_eval_fluxes", "mmf_eval_splitting",
+    "mmf_eval_bc_values",
+]
+
+
+class Grid(C.Structure):
+    _fields_ = [("dim", C.c_int), ("n", C.c_int * 3), ("origin", C.c_double * 3), ("h", C.c_double),
+                ("bc_lo", C.c_int * 3), ("bc_hi", C.c_int * 3), ("dirichlet_prim", C.c_double * 5),
+                ("order", C.c_int), ("arith", C.c_int), ("chunk", C.c_int)]
+
+
+class MMFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("mmf error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+
+
+def load(build_if_missing=True):
+    """Load libmmf_gb300.so (building it in-tree first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB_PATH) or not _build.up_to_date():
+        if not build_if_missing:
+            raise RuntimeError("libmmf_gb300.so is not built")
+        _build.build()
+    L = C.CDLL(_build.LIB_PATH)
+    L.mmf_last_error.restype = C.c_char_p
+    L.mmf_launch_count.restype = C.c_int64
+    L.mmf_launch_count.argtypes = [_P]
+    L.mmf_create.argtypes = [C.POINTER(Grid), C.c_int, C.POINTER(_P)]
+    L.mmf_destroy.argtypes = [_P]
+    L.mmf_set_cell_map.argtypes = [_P, C.c_int64, C.POINTER(C.c_int64)]
+    for name in ("mmf_upload_state", "mmf_download_state", "mmf_upload_state_device", "mmf_download_state_device"):
+        getattr(L, name).argtypes = [_P, _P, C.c_int64]
+    L.mmf_compute_rhs.argtypes = [_P, _P, _P, _D, C.c_int64]
+    L.mmf_compute_polynomials.argtypes = [_P]
+    L.mmf_time_setup.argtypes = [_P, C.c_double, C.c_double, C.c_double, C.c_int64]
+    L.mmf_advance.argtypes = [_P, C.c_int64, _D, C.POINTER(C.c_int64)]
+    L.mmf_advance_async.argtypes = [_P, C.c_int64]
+    L.mmf_time_info.argtypes = [_P, _D, C.POINTER(C.c_int64)]
+    L.mmf_get_stream.argtypes = [_P]
+    L.mmf_get_stream.restype = C.c_void_p
+    L.mmf_advance_host.argtypes = [_P, _P, C.c_int64, C.c_int64, _D]
+    L.mmf_last_step_info.argtypes = [_P, _D, _D]
+    L.mmf_get_status.argtypes = [_P, C.POINTER(C.c_uint)]
+    L.mmf_synchronize.argtypes = [_P]
+    L.mmf_rk_stage.argtypes = [_P, C.c_int]
+    L.mmf_cons2prim.argtypes = [C.c_int64, _P, _P]
+    L.mmf_prim2cons.argtypes = [C.c_int64, _P, _P]
+    L.mmf_eval_fluxes.argtypes = [C.c_int64, _P, _P, _P, _P]
+    L.mmf_eval_splitting.argtypes = [C.c_int64, _P, _P, _P, _P, _P]
+    L.mmf_eval_bc_values.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P]
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != MMF_OK:
+        raise MMFError(rc, load().mmf_last_error().decode(errors="replace"))
+    return rc
+
+
+def ptr(a):
+    """Raw pointer of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(a.ctypes.data)

@@ -1,0 +1,533 @@
+// mmf_capi.cu -- the C ABI (include/mmf_gb300.h): context, state transfer
+// between the reference's AoS raw layout and the device SoA planes, the
+// reference entry points, and the CUDA-graph time loop.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/mmf_gb300.h"
+#include "mmf_launch.cuh"
+
+using namespace mmf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define MMF_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(MMF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+constexpr int GRAPH_STEPS = 16;
+
+// AoS [n_raw][5] (raw order) -> SoA planes (grid order)
+__global__ void aos_to_soa_kernel(const double *__restrict__ aos, double *__restrict__ soa, long long n_raw,
+                                  long long plane, const long long *__restrict__ raw_to_cell)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n_raw) return;
+    const long long g = raw_to_cell ? raw_to_cell[r] : r;
+    if (g < 0 || g >= plane) return;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) soa[k * plane + g] = aos[NF * r + k];
+}
+
+__global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__restrict__ aos, long long n_raw,
+                                  long long plane, const long long *__restrict__ raw_to_cell)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n_raw) return;
+    const long long g = raw_to_cell ? raw_to_cell[r] : r;
+    if (g < 0 || g >= plane) return;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) aos[NF * r + k] = soa[k * plane + g];
+}
+
+} // namespace
+
+struct mmf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    mmf_grid grid;
+    GridParams gp;
+    double *U = nullptr, *R = nullptr, *W = nullptr;   // SoA [5][plane]
+    double *S = nullptr;                               // scratch state (compute_rhs)
+    double *aos = nullptr;                             // AoS staging [plane][5]
+    long long *raw_to_cell = nullptr;                  // null = identity
+    Ctrl *ctrl = nullptr;
+    double *rhs_maxeig = nullptr;
+    cudaGraphExec_t graph_many = nullptr, graph_one = nullptr;
+    long long launches = 0;
+    double cfl = 0.0;
+    bool time_ready = false;
+
+    cudaError_t stage(int st, const double *U_in, double *out)
+    {
+        StageArgs sa;
+        sa.U = U_in;
+        sa.R = R;
+        sa.W = W;
+        sa.out = out;
+        sa.ctrl = ctrl;
+        sa.rhs_maxeig = rhs_maxeig;
+        ++launches;
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_stage_fast(st, gp, sa, stream)
+                                                                : launch_stage_exact(st, gp, sa, stream);
+    }
+    cudaError_t rk_step()
+    {
+        cudaError_t e;
+        if ((e = stage(STAGE_1, U, R)) != cudaSuccess) return e;
+        if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
+        return stage(STAGE_3, U, U);
+    }
+};
+
+static int check_ctx(mmf_ctx *ctx)
+{
+    if (!ctx) return fail(MMF_ERR_ARG, "null context");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
+    return MMF_OK;
+}
+
+extern "C" {
+
+const char *mmf_last_error(void) { return g_last_error.c_str(); }
+int mmf_abi_version(void) { return MMF_ABI_VERSION; }
+int64_t mmf_launch_count(const mmf_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
+{
+    if (!grid || !out) return fail(MMF_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (grid->dim != 2 && grid->dim != 3) return fail(MMF_ERR_ARG, "dim must be 2 or 3");
+    for (int d = 0; d < grid->dim; ++d) {
+        if (grid->n[d] < 1) return fail(MMF_ERR_ARG, "cells per direction must be >= 1");
+        const bool plo = grid->bc_lo[d] == MMF_BC_PERIODIC, phi = grid->bc_hi[d] == MMF_BC_PERIODIC;
+        if (plo != phi) return fail(MMF_ERR_ARG, "periodic borders must be paired");
+        for (int s = 0; s < 2; ++s) {
+            const int bc = s ? grid->bc_hi[d] : grid->bc_lo[d];
+            if (bc != MMF_BC_FREE_FLOW && bc != MMF_BC_REFLECTING && bc != MMF_BC_WALL && bc != MMF_BC_DIRICHLET &&
+                bc != MMF_BC_PERIODIC)
+                return fail(MMF_ERR_ARG, "unknown border condition");
+        }
+    }
+    if (!(grid->h > 0.0)) return fail(MMF_ERR_ARG, "h must be > 0");
+    if (grid->order != 1)   // src/reconstruction.cpp:75-76 exits on any other order
+        return fail(MMF_ERR_UNSUPPORTED, "only order 1 is supported by this context type");
+    if (grid->arith != MMF_ARITH_REFERENCE && grid->arith != MMF_ARITH_FAST)
+        return fail(MMF_ERR_ARG, "unknown arithmetic");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+        return fail(MMF_ERR_CUDA, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(MMF_ERR_ARG, "device index out of range");
+    MMF_CUDA(cudaSetDevice(device));
+
+    mmf_ctx *c = new mmf_ctx();
+    c->device = device;
+    c->grid = *grid;
+    if (grid->dim == 2) c->grid.n[2] = 1;
+    GridParams &gp = c->gp;
+    memset(&gp, 0, sizeof(gp));
+    gp.dim = grid->dim;
+    for (int d = 0; d < 3; ++d) {
+        gp.n[d] = c->grid.n[d];
+        gp.bc_lo[d] = (d < grid->dim) ? grid->bc_lo[d] : MMF_BC_FREE_FLOW;
+        gp.bc_hi[d] = (d < grid->dim) ? grid->bc_hi[d] : MMF_BC_FREE_FLOW;
+    }
+    for (int k = 0; k < NF; ++k) gp.dir_prim[k] = grid->dirichlet_prim[k];
+    const double h = grid->h;
+    gp.area = (grid->dim == 3) ? h * h : h;
+    gp.vol = (grid->dim == 3) ? h * h * h : h * h;
+    plan_cartesian(gp, grid->chunk);
+    const size_t bytes = sizeof(double) * NF * (size_t)gp.plane;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->U, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->R, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->W, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->aos, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ctrl, sizeof(Ctrl));
+    if (e == cudaSuccess) e = cudaMalloc(&c->rhs_maxeig, sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->U, 0, bytes, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->ctrl, 0, sizeof(Ctrl), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        std::string msg = cudaGetErrorString(e);
+        mmf_destroy(c);
+        return fail(e == cudaErrorMemoryAllocation ? MMF_ERR_NOMEM : MMF_ERR_CUDA, msg);
+    }
+    *out = c;
+    return MMF_OK;
+}
+
+int mmf_destroy(mmf_ctx *c)
+{
+    if (!c) return MMF_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
+    if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+    cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
+    cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MMF_OK;
+}
+
+int mmf_set_cell_map(mmf_ctx *c, int64_t n_raw, const int64_t *raw_to_cell)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "n_raw must equal the cell count");
+    if (!raw_to_cell) {
+        cudaFree(c->raw_to_cell);
+        c->raw_to_cell = nullptr;
+        return MMF_OK;
+    }
+    // must be a permutation of the grid cells
+    std::string seen((size_t)n_raw, '\0');
+    for (int64_t r = 0; r < n_raw; ++r) {
+        const int64_t g = raw_to_cell[r];
+        if (g < 0 || g >= n_raw || seen[(size_t)g]) return fail(MMF_ERR_ARG, "cell map is not a permutation");
+        seen[(size_t)g] = 1;
+    }
+    if (!c->raw_to_cell) MMF_CUDA(cudaMalloc(&c->raw_to_cell, sizeof(long long) * n_raw));
+    MMF_CUDA(cudaMemcpyAsync(c->raw_to_cell, raw_to_cell, sizeof(long long) * n_raw, cudaMemcpyHostToDevice,
+                             c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+static int to_soa(mmf_ctx *c, const double *d_aos, double *soa, int64_t n_raw)
+{
+    const unsigned blocks = (unsigned)((n_raw + 255) / 256);
+    aos_to_soa_kernel<<<blocks, 256, 0, c->stream>>>(d_aos, soa, n_raw, c->gp.plane, c->raw_to_cell);
+    ++c->launches;
+    MMF_CUDA(cudaPeekAtLastError());
+    return MMF_OK;
+}
+
+static int from_soa(mmf_ctx *c, const double *soa, double *d_aos, int64_t n_raw)
+{
+    const unsigned blocks = (unsigned)((n_raw + 255) / 256);
+    soa_to_aos_kernel<<<blocks, 256, 0, c->stream>>>(soa, d_aos, n_raw, c->gp.plane, c->raw_to_cell);
+    ++c->launches;
+    MMF_CUDA(cudaPeekAtLastError());
+    return MMF_OK;
+}
+
+int mmf_upload_state(mmf_ctx *c, const double *aos, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    MMF_CUDA(cudaMemcpyAsync(c->aos, aos, sizeof(double) * NF * n_raw, cudaMemcpyHostToDevice, c->stream));
+    return to_soa(c, c->aos, c->U, n_raw);
+}
+
+int mmf_download_state(mmf_ctx *c, double *aos, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    if ((rc = from_soa(c, c->U, c->aos, n_raw))) return rc;
+    MMF_CUDA(cudaMemcpyAsync(aos, c->aos, sizeof(double) * NF * n_raw, cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_upload_state_device(mmf_ctx *c, const double *d_aos, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!d_aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    return to_soa(c, d_aos, c->U, n_raw);
+}
+
+int mmf_download_state_device(mmf_ctx *c, double *d_aos, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!d_aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    return from_soa(c, c->U, d_aos, n_raw);
+}
+
+int mmf_compute_rhs(mmf_ctx *c, const double *cons, double *rhs, double *max_eig, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!cons || !rhs || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad buffers");
+    const size_t bytes = sizeof(double) * NF * (size_t)n_raw;
+    if (!c->S) MMF_CUDA(cudaMalloc(&c->S, bytes));
+    MMF_CUDA(cudaMemcpyAsync(c->aos, cons, bytes, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = to_soa(c, c->aos, c->S, n_raw))) return rc;
+    MMF_CUDA(cudaMemsetAsync(c->rhs_maxeig, 0, sizeof(double), c->stream));
+    // the residual of stage 'RHS' lands in R; S is the input state
+    {
+        StageArgs sa;
+        sa.U = c->S; sa.R = c->R; sa.W = c->W; sa.out = c->R; sa.ctrl = c->ctrl; sa.rhs_maxeig = c->rhs_maxeig;
+        ++c->launches;
+        MMF_CUDA(launch_stage_exact(STAGE_RHS, c->gp, sa, c->stream));
+    }
+    if ((rc = from_soa(c, c->R, c->aos, n_raw))) return rc;
+    MMF_CUDA(cudaMemcpyAsync(rhs, c->aos, bytes, cudaMemcpyDeviceToHost, c->stream));
+    double me = 0.0;
+    MMF_CUDA(cudaMemcpyAsync(&me, c->rhs_maxeig, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (max_eig) *max_eig = me;
+    return MMF_OK;
+}
+
+int mmf_compute_polynomials(mmf_ctx *c)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    return MMF_OK;   // order 1: src/reconstruction.cpp:47-55 is empty
+}
+
+int mmf_time_setup(mmf_ctx *c, double cfl, double t, double t_end, int64_t max_steps)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!(cfl > 0.0)) return fail(MMF_ERR_ARG, "CFL must be > 0");
+    if (std::isinf(t_end) && max_steps < 0) return fail(MMF_ERR_ARG, "infinite end time needs max_steps");
+    Ctrl h;
+    memset(&h, 0, sizeof(h));
+    h.t = t;
+    h.t_end = t_end;
+    h.cfl_h = 0.9 * cfl * c->grid.h;
+    h.max_steps = (max_steps < 0) ? LLONG_MAX : max_steps;
+    MMF_CUDA(cudaMemcpyAsync(c->ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    c->cfl = cfl;
+    c->time_ready = true;
+    return MMF_OK;
+}
+
+static int build_graph(mmf_ctx *c, int steps, cudaGraphExec_t *exec)
+{
+    cudaGraph_t g = nullptr;
+    MMF_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaSuccess;
+    const long long before = c->launches;
+    for (int s = 0; s < steps && err == cudaSuccess; ++s) err = c->rk_step();
+    c->launches = before;   // captured, not executed
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (err != cudaSuccess) { if (g) cudaGraphDestroy(g); return fail(MMF_ERR_CUDA, cudaGetErrorString(err)); }
+    if (e2 != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e2));
+    cudaError_t e3 = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e3));
+    return MMF_OK;
+}
+
+int mmf_advance(mmf_ctx *c, int64_t n_steps, double *t_out, int64_t *steps_done)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    if (n_steps < 0) return fail(MMF_ERR_ARG, "n_steps < 0");
+    if (!c->graph_many && (rc = build_graph(c, GRAPH_STEPS, &c->graph_many))) return rc;
+    if (!c->graph_one && (rc = build_graph(c, 1, &c->graph_one))) return rc;
+    Ctrl before;
+    MMF_CUDA(cudaMemcpyAsync(&before, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    int64_t left = n_steps;
+    while (left >= GRAPH_STEPS) {
+        MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
+        c->launches += 3 * GRAPH_STEPS;
+        left -= GRAPH_STEPS;
+    }
+    while (left-- > 0) {
+        MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
+        c->launches += 3;
+    }
+    Ctrl after;
+    MMF_CUDA(cudaMemcpyAsync(&after, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (t_out) *t_out = after.t;
+    if (steps_done) *steps_done = after.step - before.step;
+    if (after.status) return fail(MMF_ERR_STATE, "non-physical state (negative density/pressure or NaN)");
+    return MMF_OK;
+}
+
+int mmf_advance_async(mmf_ctx *c, int64_t n_steps)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    if (n_steps < 0) return fail(MMF_ERR_ARG, "n_steps < 0");
+    if (!c->graph_many && (rc = build_graph(c, GRAPH_STEPS, &c->graph_many))) return rc;
+    if (!c->graph_one && (rc = build_graph(c, 1, &c->graph_one))) return rc;
+    int64_t left = n_steps;
+    while (left >= GRAPH_STEPS) {
+        MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
+        c->launches += 3 * GRAPH_STEPS;
+        left -= GRAPH_STEPS;
+    }
+    while (left-- > 0) {
+        MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
+        c->launches += 3;
+    }
+    return MMF_OK;
+}
+
+int mmf_time_info(mmf_ctx *c, double *t, int64_t *step)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    Ctrl h;
+    MMF_CUDA(cudaMemcpyAsync(&h, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (t) *t = h.t;
+    if (step) *step = h.step;
+    return MMF_OK;
+}
+
+void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int mmf_advance_host(mmf_ctx *c, double *aos, int64_t n_raw, int64_t n_steps, double *t_out)
+{
+    int rc = mmf_upload_state(c, aos, n_raw);
+    if (rc) return rc;
+    int64_t done = 0;
+    rc = mmf_advance(c, n_steps, t_out, &done);
+    if (rc && rc != MMF_ERR_STATE) return rc;
+    int rc2 = mmf_download_state(c, aos, n_raw);
+    return rc ? rc : rc2;
+}
+
+int mmf_rk_stage(mmf_ctx *c, int stage)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    cudaError_t e;
+    switch (stage) {
+    case 1: e = c->stage(STAGE_1, c->U, c->R); break;
+    case 2: e = c->stage(STAGE_2, c->U, c->W); break;
+    case 3: e = c->stage(STAGE_3, c->U, c->U); break;
+    default: return fail(MMF_ERR_ARG, "stage must be 1, 2 or 3");
+    }
+    if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
+    return MMF_OK;
+}
+
+int mmf_last_step_info(mmf_ctx *c, double *dt, double *max_eig)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    Ctrl h;
+    MMF_CUDA(cudaMemcpyAsync(&h, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (dt) *dt = h.dt;
+    if (max_eig) *max_eig = h.last_maxeig;
+    return MMF_OK;
+}
+
+int mmf_get_status(mmf_ctx *c, unsigned *status)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    Ctrl h;
+    MMF_CUDA(cudaMemcpyAsync(&h, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (status) *status = h.status;
+    const unsigned zero = 0;
+    MMF_CUDA(cudaMemcpyAsync((char *)c->ctrl + offsetof(Ctrl, status), &zero, sizeof(unsigned),
+                             cudaMemcpyHostToDevice, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_synchronize(mmf_ctx *c)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+// ---- unit-level functions ------------------------------------------------
+
+static int pointwise(int op, int64_t n, const double *a, const double *b, const double *nrm, int bc,
+                     const double *dir_prim, double *out, double *out2)
+{
+    if (n < 0) return fail(MMF_ERR_ARG, "n < 0");
+    if (n == 0) return MMF_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(MMF_ERR_CUDA, "no CUDA device available");
+    const size_t s5 = sizeof(double) * NF * (size_t)n, s3 = sizeof(double) * 3 * (size_t)n;
+    double *da = nullptr, *db = nullptr, *dn = nullptr, *dp = nullptr, *dout = nullptr, *dout2 = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&da, s5);
+    if (e == cudaSuccess && b) e = cudaMalloc(&db, s5);
+    if (e == cudaSuccess && nrm) e = cudaMalloc(&dn, s3);
+    if (e == cudaSuccess && dir_prim) e = cudaMalloc(&dp, sizeof(double) * NF);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, s5);
+    if (e == cudaSuccess && out2) e = cudaMalloc(&dout2, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(da, a, s5, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && b) e = cudaMemcpyAsync(db, b, s5, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nrm) e = cudaMemcpyAsync(dn, nrm, s3, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && dir_prim) e = cudaMemcpyAsync(dp, dir_prim, sizeof(double) * NF, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_pointwise_exact(op, n, da, db, dn, bc, dp, dout, dout2, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, s5, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && out2) e = cudaMemcpyAsync(out2, dout2, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(da); cudaFree(db); cudaFree(dn); cudaFree(dp); cudaFree(dout); cudaFree(dout2);
+    if (s) cudaStreamDestroy(s);
+    if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
+    return MMF_OK;
+}
+
+int mmf_cons2prim(int64_t n, const double *cons, double *prim)
+{
+    if (!cons || !prim) return fail(MMF_ERR_ARG, "null buffer");
+    return pointwise(OP_CONS2PRIM, n, cons, nullptr, nullptr, 0, nullptr, prim, nullptr);
+}
+
+int mmf_prim2cons(int64_t n, const double *prim, double *cons)
+{
+    if (!cons || !prim) return fail(MMF_ERR_ARG, "null buffer");
+    return pointwise(OP_PRIM2CONS, n, prim, nullptr, nullptr, 0, nullptr, cons, nullptr);
+}
+
+int mmf_eval_fluxes(int64_t n, const double *cons, const double *prim, const double *normal, double *flux)
+{
+    if (!cons || !prim || !normal || !flux) return fail(MMF_ERR_ARG, "null buffer");
+    return pointwise(OP_FLUXES, n, cons, prim, normal, 0, nullptr, flux, nullptr);
+}
+
+int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, const double *normal, double *flux,
+                       double *lambda)
+{
+    if (!cons_l || !cons_r || !normal || !flux || !lambda) return fail(MMF_ERR_ARG, "null buffer");
+    return pointwise(OP_SPLITTING, n, cons_l, cons_r, normal, 0, nullptr, flux, lambda);
+}
+
+int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
+                       const double *dirichlet_prim, double *cons_bc)
+{
+    if (!normal || !cons || !cons_bc) return fail(MMF_ERR_ARG, "null buffer");
+    if (bc_type != MMF_BC_FREE_FLOW && bc_type != MMF_BC_REFLECTING && bc_type != MMF_BC_WALL &&
+        bc_type != MMF_BC_DIRICHLET)
+        return fail(MMF_ERR_ARG, "unknown border condition");
+    if (bc_type == MMF_BC_DIRICHLET && !dirichlet_prim) return fail(MMF_ERR_ARG, "Dirichlet needs a state");
+    return pointwise(OP_BC, n, cons, nullptr, normal, bc_type, dirichlet_prim, cons_bc, nullptr);
+}
+
+} // extern "C"

@@ -1,0 +1,436 @@
+// mmf_cartesian.cuh -- fused SSP-RK3 stage kernels on a uniform Cartesian grid
+// (order-1 reconstruction), FP64, structure-of-arrays state.
+//
+// One launch per Runge-Kutta stage computes, for every cell it owns, the
+// residual of euler::computeRHS (euler.cpp:127-249) and applies the stage
+// combination of main.cpp:409-495, so the residual never round-trips HBM
+// except between stage 1 and stage 2 (dt is only known after stage 1's
+// maxEig reduction):
+//   stage 1:  R1 = RHS(U);                       maxEig -> ctrl (atomicMax)
+//   stage 2:  W1 = U + dt R1 / V (recomputed on the fly, halo included)
+//             W2 = 3/4 U + 1/4 (W1 + dt RHS(W1) / V)
+//   stage 3:  U  = 1/3 U + 2/3 (W2 + dt RHS(W2) / V)      (in place)
+// 320 bytes of HBM traffic per cell and step (8 reads/writes x 5 fields x 8 B).
+//
+// Work decomposition.  A warp owns 30 consecutive cells of a grid row and
+// evaluates 32 (one halo cell each side), so x-face states move between lanes
+// by shuffles.  In 2D the warp marches up the rows of a chunk and carries the
+// previous row's record and y-face flux in registers; in 3D a block stacks
+// BY warps in y (halo rows at both ends exchange through shared memory) and
+// marches along z.  Each face flux is evaluated once per owning warp.
+//
+// Per-cell accumulation order is the reference's: for each direction, the
+// low face then the high face (the interface list is x-faces, y-faces,
+// z-faces), except that a periodic wrap face comes first for the last cell
+// of the line.  Border faces are evaluated as split(ghost, U, +e_d), which
+// is the exact negation of the reference's split(U, ghost, -e_d).
+#pragma once
+
+#include "mmf_physics.cuh"
+
+namespace mmf {
+
+struct Ctrl {
+    double t;
+    double t_end;
+    double dt;
+    double cfl_h;                   // 0.9 * cfl * minCellSize   (main.cpp:398)
+    unsigned long long maxeig_bits; // stage-1 max eigenvalue (non-negative double bits)
+    long long step;
+    long long max_steps;
+    int active;                     // this step runs (t < t_end and step < max_steps)
+    unsigned status;                // bit0 rho<0, bit1 p<0, bit2 NaN
+    double last_maxeig;             // stage-1 maxEig of the last step (log)
+};
+
+struct GridParams {
+    int dim;
+    int n[3];
+    int bc_lo[3], bc_hi[3];
+    double dir_prim[NF];
+    double area, vol;
+    int chunk;      // rows (2D) / planes (3D) per marching chunk
+    int nseg;       // x segments of 30 cells
+    int nrowblk;    // 3D: row blocks in y
+    int nchunk;
+    long long plane;  // cells per field plane
+};
+
+struct StageArgs {
+    const double *U;     // state at the start of the step
+    const double *R;     // stage-1 residual
+    const double *W;     // stage-2 result
+    double *out;         // this stage's output
+    Ctrl *ctrl;
+    double *rhs_maxeig;  // stage 0 (residual only): max eigenvalue output
+};
+
+constexpr int SEG = 30;   // output cells per warp row
+
+enum { STAGE_RHS = 0, STAGE_1 = 1, STAGE_2 = 2, STAGE_3 = 3 };
+
+template <class A> struct IsExact { static constexpr bool value = false; };
+template <> struct IsExact<ExactArith> { static constexpr bool value = true; };
+
+__device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Per-launch step scalars.
+struct StepScalars {
+    double dt;     // time step (stages 2, 3)
+    double s;      // stage scale: exact dt (then / V), fast 0.5*A*dt/V
+    bool active;
+};
+
+template <class A, int STAGE>
+__device__ __forceinline__ StepScalars step_scalars(const GridParams &gp, const Ctrl *ctrl)
+{
+    StepScalars sc;
+    sc.dt = 0.0;
+    sc.s = 0.0;
+    if (STAGE == STAGE_RHS) { sc.active = true; return sc; }
+    if (STAGE == STAGE_1) {
+        sc.active = (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps);
+        return sc;
+    }
+    sc.active = ctrl->active != 0;
+    if (STAGE == STAGE_2) {
+        // main.cpp:398-402
+        double maxEig = __longlong_as_double((long long)ctrl->maxeig_bits);
+        double dt = ctrl->cfl_h / maxEig;
+        if (ctrl->t + dt > ctrl->t_end) dt = ctrl->t_end - ctrl->t;
+        sc.dt = dt;
+    } else {
+        sc.dt = ctrl->dt;
+    }
+    sc.s = IsExact<A>::value ? sc.dt : 0.5 * gp.area * sc.dt / gp.vol;
+    return sc;
+}
+
+// Control-block updates made once per launch by thread 0 of block 0.  No
+// other block of the same launch reads the fields written here: stage 2 and
+// stage 3 read only 'active' and 'dt' (stage 2 recomputes dt from maxEig).
+template <int STAGE>
+__device__ __forceinline__ void step_bookkeeping(Ctrl *ctrl, const StepScalars &sc)
+{
+    if (STAGE == STAGE_1) ctrl->active = sc.active ? 1 : 0;
+    if (!sc.active) return;
+    if (STAGE == STAGE_2) ctrl->dt = sc.dt;
+    if (STAGE == STAGE_3) {
+        // main.cpp:505-506; the stage-1 reduction slot is cleared for the next step
+        ctrl->last_maxeig = __longlong_as_double((long long)ctrl->maxeig_bits);
+        ctrl->t += sc.dt;
+        ctrl->step += 1;
+        ctrl->maxeig_bits = 0ull;
+    }
+}
+
+// Stage input state of grid cell g.
+template <class A, int STAGE>
+__device__ __forceinline__ void load_state(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                           long long g, double *c)
+{
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        const long long o = (long long)k * gp.plane + g;
+        if (STAGE == STAGE_2) {
+            const double u = __ldg(sa.U + o), r = __ldg(sa.R + o);
+            if (IsExact<A>::value) c[k] = u + sc.dt * r / gp.vol;   // main.cpp:421
+            else c[k] = fma(sc.s, r, u);
+        } else if (STAGE == STAGE_3) {
+            c[k] = __ldg(sa.W + o);
+        } else {
+            c[k] = __ldg(sa.U + o);
+        }
+    }
+}
+
+// Stage output of grid cell g from its residual accumulator and stage state.
+template <class A, int STAGE>
+__device__ __forceinline__ void store_output(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                             long long g, const double *acc, const double *cstate)
+{
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        const long long o = (long long)k * gp.plane + g;
+        double v;
+        if (STAGE == STAGE_RHS || STAGE == STAGE_1) {
+            v = acc[k];
+        } else if (STAGE == STAGE_2) {
+            const double u = __ldg(sa.U + o);
+            if (IsExact<A>::value) v = 0.75 * u + 0.25 * (cstate[k] + sc.dt * acc[k] / gp.vol); // main.cpp:457
+            else v = fma(0.25, fma(sc.s, acc[k], cstate[k]), 0.75 * u);
+        } else {
+            const double u = sa.out[o];   // in place: U
+            if (IsExact<A>::value) v = (1. / 3) * u + (2. / 3) * (cstate[k] + sc.dt * acc[k] / gp.vol); // main.cpp:493
+            else v = fma(2.0 / 3.0, fma(sc.s, acc[k], cstate[k]), u * (1.0 / 3.0));
+        }
+        sa.out[o] = v;
+    }
+}
+
+// Adds the two faces of direction d to the accumulator in reference order.
+template <class A>
+__device__ __forceinline__ void accumulate_pair(double *acc, const double *Flo, const double *Fhi, double area,
+                                                bool hi_first)
+{
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        if (IsExact<A>::value) {
+            if (hi_first) { acc[k] = acc[k] - area * Fhi[k]; acc[k] = acc[k] + area * Flo[k]; }
+            else { acc[k] = acc[k] + area * Flo[k]; acc[k] = acc[k] - area * Fhi[k]; }
+        } else {
+            acc[k] += Flo[k] - Fhi[k];
+        }
+    }
+}
+
+// Column (or row) index along one direction with border handling:
+// returns the interior index to load and sets ghost = -1/+1 for a border ghost.
+__device__ __forceinline__ int resolve_index(int i, int n, bool periodic, int &ghost)
+{
+    ghost = 0;
+    if (i < 0) {
+        if (periodic) return n - 1;
+        ghost = -1;
+        return 0;
+    }
+    if (i >= n) {
+        if (periodic) return (i - n < n) ? i - n : n - 1;
+        if (i == n) ghost = 1;
+        return n - 1;
+    }
+    return i;
+}
+
+// Record of the cell at (x, y, z) (may be a ghost) for this stage.
+template <class A, int STAGE, int DIM>
+__device__ __forceinline__ void load_record(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                            int x, int y, int z, CellRec<DIM> &r, unsigned *status)
+{
+    int gx, gy, gz = 0;
+    const int ix = resolve_index(x, gp.n[0], gp.bc_lo[0] == BC_PERIODIC, gx);
+    const int iy = resolve_index(y, gp.n[1], gp.bc_lo[1] == BC_PERIODIC, gy);
+    const int iz = (DIM == 3) ? resolve_index(z, gp.n[2], gp.bc_lo[2] == BC_PERIODIC, gz) : 0;
+    const long long g = (long long)ix + (long long)gp.n[0] * ((long long)iy + (long long)gp.n[1] * iz);
+    load_state<A, STAGE>(sa, gp, sc, g, r.c);
+    const bool ghost = (gx | gy | gz) != 0;
+    if (ghost) {
+        if (gx) {
+            const double n[3] = {(double)gx, 0.0, 0.0};
+            double t[NF];
+            ghost_state<A>(gx < 0 ? gp.bc_lo[0] : gp.bc_hi[0], n, r.c, gp.dir_prim, t);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+        }
+        if (gy) {
+            const double n[3] = {0.0, (double)gy, 0.0};
+            double t[NF];
+            ghost_state<A>(gy < 0 ? gp.bc_lo[1] : gp.bc_hi[1], n, r.c, gp.dir_prim, t);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+        }
+        if (DIM == 3 && gz) {
+            const double n[3] = {0.0, 0.0, (double)gz};
+            double t[NF];
+            ghost_state<A>(gz < 0 ? gp.bc_lo[2] : gp.bc_hi[2], n, r.c, gp.dir_prim, t);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+        }
+    }
+    A::template record<DIM>(r, ghost ? nullptr : status);
+}
+
+// Face between record L (this lane) and record R along direction d.
+template <class A, int DIM>
+__device__ __forceinline__ double face_dir(const CellRec<DIM> &L, const CellRec<DIM> &R, int d, double *F)
+{
+    return A::face(L.c, L.f[d], L.lam[d], R.c, R.f[d], R.lam[d], F);
+}
+
+// x-faces of a warp row: Fhi = face(lane, lane+1), Flo = face(lane-1, lane).
+template <class A, int DIM>
+__device__ __forceinline__ double xfaces(const CellRec<DIM> &r, double *Flo, double *Fhi)
+{
+    double cR[NF], fR[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) { cR[k] = shfl_down(r.c[k], 1); fR[k] = shfl_down(r.f[0][k], 1); }
+    const double lamR = shfl_down(r.lam[0], 1);
+    const double lam = A::face(r.c, r.f[0], r.lam[0], cR, fR, lamR, Fhi);
+#pragma unroll
+    for (int k = 0; k < NF; ++k) Flo[k] = shfl_up(Fhi[k], 1);
+    return lam;
+}
+
+// ---------------------------------------------------------------- 2D kernel
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs sa)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (warp >= gp.nseg * gp.nchunk) return;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+
+    const int nx = gp.n[0], ny = gp.n[1];
+    const int seg = warp % gp.nseg, chunk = warp / gp.nseg;
+    const int x = seg * SEG - 1 + lane;
+    const int y0 = chunk * gp.chunk;
+    const int y1 = min(y0 + gp.chunk, ny);
+    const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
+    const bool xface_valid = (lane <= SEG) && (x < nx);
+    const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC;
+    unsigned status = 0;
+    unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
+    double lmax = 0.0;
+
+    CellRec<2> cur, abv;
+    double Fylo[NF], Fyhi[NF], Fxlo[NF], Fxhi[NF], acc[NF];
+    load_record<A, STAGE, 2>(sa, gp, sc, x, y0 - 1, 0, abv, nullptr);
+    load_record<A, STAGE, 2>(sa, gp, sc, x, y0, 0, cur, st);
+    {
+        const double l = face_dir<A, 2>(abv, cur, 1, Fylo);
+        if (out_col) lmax = fmax(lmax, l);
+    }
+    for (int y = y0; y < y1; ++y) {
+        load_record<A, STAGE, 2>(sa, gp, sc, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
+        const double ly = face_dir<A, 2>(cur, abv, 1, Fyhi);
+        const double lx = xfaces<A, 2>(cur, Fxlo, Fxhi);
+        if (STAGE <= STAGE_1) {
+            if (out_col) lmax = fmax(lmax, ly);
+            if (xface_valid) lmax = fmax(lmax, lx);
+        }
+        if (out_col) {
+#pragma unroll
+            for (int k = 0; k < NF; ++k) acc[k] = 0.0;
+            accumulate_pair<A>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
+            accumulate_pair<A>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
+            store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * y, acc, cur.c);
+        }
+        cur = abv;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) Fylo[k] = Fyhi[k];
+    }
+    if (STAGE <= STAGE_1) {
+        lmax = warp_max(lmax);
+        if (lane == 0) {
+            unsigned long long* dst = (STAGE == STAGE_RHS) ? (unsigned long long*)sa.rhs_maxeig : &sa.ctrl->maxeig_bits;
+            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        }
+        if (STAGE == STAGE_1) {
+            status = __reduce_or_sync(0xffffffffu, status);
+            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- 3D kernel
+// Block = BY warps stacked in y (rows y0-1 .. y0+BY-2; the first and last are
+// halo rows that only contribute y-face states), marching along z.
+template <int BY>
+struct Smem3D {
+    double c[BY][NF][32];
+    double f[BY][NF][32];
+    double lam[BY][32];
+    double F[BY][NF][32];
+};
+
+template <class A, int STAGE, int BY>
+__global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageArgs sa)
+{
+    __shared__ Smem3D<BY> sm;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    int b = blockIdx.x;
+    const int seg = b % gp.nseg; b /= gp.nseg;
+    const int rb = b % gp.nrowblk; b /= gp.nrowblk;
+    const int chunk = b;
+    const int x = seg * SEG - 1 + lane;
+    const int y = rb * (BY - 2) - 1 + w;
+    const int z0 = chunk * gp.chunk;
+    const int z1 = min(z0 + gp.chunk, nz);
+    const bool halo_row = (w == 0) || (w == BY - 1);
+    const bool out_row = !halo_row && (y < ny);
+    const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
+    const bool out = out_row && out_col;
+    const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
+               perz = gp.bc_lo[2] == BC_PERIODIC;
+    unsigned status = 0;
+    unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
+    double lmax = 0.0;
+
+    CellRec<3> cur, abv;
+    double Fzlo[NF], Fzhi[NF], Fxlo[NF], Fxhi[NF], Fylo[NF], Fyhi[NF], acc[NF];
+    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, abv, nullptr);
+    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
+    {
+        const double l = face_dir<A, 3>(abv, cur, 2, Fzlo);
+        if (out) lmax = fmax(lmax, l);
+    }
+    for (int z = z0; z < z1; ++z) {
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, abv, (z + 1 < z1) ? st : nullptr);
+        const double lz = face_dir<A, 3>(cur, abv, 2, Fzhi);
+        const double lx = xfaces<A, 3>(cur, Fxlo, Fxhi);
+        // y-faces through shared memory
+#pragma unroll
+        for (int k = 0; k < NF; ++k) { sm.c[w][k][lane] = cur.c[k]; sm.f[w][k][lane] = cur.f[1][k]; }
+        sm.lam[w][lane] = cur.lam[1];
+        __syncthreads();
+        double ly = 0.0;
+        if (w < BY - 1) {
+            double cR[NF], fR[NF];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) { cR[k] = sm.c[w + 1][k][lane]; fR[k] = sm.f[w + 1][k][lane]; }
+            ly = A::face(cur.c, cur.f[1], cur.lam[1], cR, fR, sm.lam[w + 1][lane], Fyhi);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) sm.F[w][k][lane] = Fyhi[k];
+        }
+        __syncthreads();
+        if (out) {
+#pragma unroll
+            for (int k = 0; k < NF; ++k) Fylo[k] = sm.F[w - 1][k][lane];
+            if (STAGE <= STAGE_1) {
+                lmax = fmax(lmax, fmax(lz, ly));
+                if (w == 1) lmax = fmax(lmax, sm.lam[0][lane] < cur.lam[1] ? cur.lam[1] : sm.lam[0][lane]);
+            }
+#pragma unroll
+            for (int k = 0; k < NF; ++k) acc[k] = 0.0;
+            accumulate_pair<A>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
+            accumulate_pair<A>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
+            accumulate_pair<A>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
+            store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
+                                   acc, cur.c);
+        }
+        if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = fmax(lmax, lx);
+        __syncthreads();
+        cur = abv;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) Fzlo[k] = Fzhi[k];
+    }
+    if (STAGE <= STAGE_1) {
+        lmax = warp_max(lmax);
+        if (lane == 0) {
+            unsigned long long* dst = (STAGE == STAGE_RHS) ? (unsigned long long*)sa.rhs_maxeig : &sa.ctrl->maxeig_bits;
+            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        }
+        if (STAGE == STAGE_1) {
+            status = __reduce_or_sync(0xffffffffu, status);
+            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
+        }
+    }
+}
+
+} // namespace mmf

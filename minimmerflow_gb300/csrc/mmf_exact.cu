@@ -1,0 +1,56 @@
+// mmf_exact.cu -- reference-arithmetic instantiation of the stage kernels and
+// the pointwise kernels of the reference's unit-level functions.  Built with
+// -fmad=false so no multiply-add is contracted: the results are the
+// reference's CPU results bit for bit.
+#include "mmf_launch.cuh"
+
+namespace mmf {
+
+cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s)
+{
+    return launch_stage<ExactArith>(stage, gp, sa, s);
+}
+
+// One thread per item; arrays are AoS [n][5] (normals [n][3]).
+__global__ void pointwise_kernel(int op, long long n, const double *a, const double *b, const double *nrm, int bc,
+                                 const double *dir_prim, double *out, double *out2)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *ai = a + NF * i;
+    double *oi = out + NF * i;
+    double dp[NF];
+    switch (op) {
+    case OP_CONS2PRIM: ExactArith::cons2prim(ai, oi); break;           // utils.cpp:48-63
+    case OP_PRIM2CONS: ExactArith::prim2cons(ai, oi); break;           // utils.cpp:71-83
+    case OP_FLUXES: ExactArith::eval_fluxes(ai, b + NF * i, nrm + 3 * i, oi); break; // euler.cpp:83-113
+    case OP_SPLITTING: {                                                // euler.cpp:42-73
+        const double *cl = ai, *cr = b + NF * i, *nn = nrm + 3 * i;
+        double pl[NF], pr[NF], fl[NF], fr[NF];
+        ExactArith::cons2prim(cl, pl);
+        ExactArith::cons2prim(cr, pr);
+        ExactArith::eval_fluxes(cl, pl, nn, fl);
+        ExactArith::eval_fluxes(cr, pr, nn, fr);
+        double lamL = fabs(ExactArith::normal_velocity(pl, nn)) + sqrt(GAMMA * pl[4]);
+        double lamR = fabs(ExactArith::normal_velocity(pr, nn)) + sqrt(GAMMA * pr[4]);
+        out2[i] = ExactArith::face(cl, fl, lamL, cr, fr, lamR, oi);
+        break;
+    }
+    case OP_BC:                                                         // euler.cpp:261-376
+        for (int k = 0; k < NF; ++k) dp[k] = dir_prim ? dir_prim[k] : 0.0;
+        ghost_state<ExactArith>(bc, nrm + 3 * i, ai, dp, oi);
+        break;
+    default: break;
+    }
+}
+
+cudaError_t launch_pointwise_exact(int op, long long n, const double *a, const double *b, const double *nrm,
+                                   int bc, const double *dir_prim, double *out, double *out2, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    pointwise_kernel<<<blocks, 128, 0, s>>>(op, n, a, b, nrm, bc, dir_prim, out, out2);
+    return cudaPeekAtLastError();
+}
+
+} // namespace mmf

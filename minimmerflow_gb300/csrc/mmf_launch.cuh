@@ -1,0 +1,71 @@
+// mmf_launch.cuh -- host-side launch shapes of the stage kernels.  Included by
+// the two arithmetic translation units (mmf_exact.cu, built with -fmad=false,
+// and mmf_fast.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mmf_cartesian.cuh"
+
+namespace mmf {
+
+constexpr int BY3D = 8;         // warps per 3D block (6 output rows + 2 halo rows)
+constexpr int WARPS_2D = 4;     // warps per 2D block
+
+// Fills the decomposition fields of gp for the given marching chunk.
+inline void plan_cartesian(GridParams &gp, int chunk)
+{
+    gp.nseg = (gp.n[0] + SEG - 1) / SEG;
+    if (gp.dim == 2) {
+        gp.chunk = chunk > 0 ? chunk : 32;
+        gp.nchunk = (gp.n[1] + gp.chunk - 1) / gp.chunk;
+        gp.nrowblk = 1;
+    } else {
+        gp.chunk = chunk > 0 ? chunk : 16;
+        gp.nchunk = (gp.n[2] + gp.chunk - 1) / gp.chunk;
+        gp.nrowblk = (gp.n[1] + BY3D - 3) / (BY3D - 2);
+    }
+    gp.plane = (long long)gp.n[0] * gp.n[1] * gp.n[2];
+}
+
+// Kernel launches this decomposition makes per stage (for launch counting).
+inline long long cartesian_blocks(const GridParams &gp)
+{
+    if (gp.dim == 2) {
+        long long warps = (long long)gp.nseg * gp.nchunk;
+        return (warps + WARPS_2D - 1) / WARPS_2D;
+    }
+    return (long long)gp.nseg * gp.nrowblk * gp.nchunk;
+}
+
+template <class A, int STAGE>
+inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cudaStream_t s)
+{
+    const unsigned blocks = (unsigned)cartesian_blocks(gp);
+    if (gp.dim == 2) stage2d_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa);
+    else stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
+    return cudaPeekAtLastError();
+}
+
+template <class A>
+inline cudaError_t launch_stage(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s)
+{
+    switch (stage) {
+    case STAGE_RHS: return launch_stage_t<A, STAGE_RHS>(gp, sa, s);
+    case STAGE_1: return launch_stage_t<A, STAGE_1>(gp, sa, s);
+    case STAGE_2: return launch_stage_t<A, STAGE_2>(gp, sa, s);
+    case STAGE_3: return launch_stage_t<A, STAGE_3>(gp, sa, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Entry points of the two arithmetic translation units.
+cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
+cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
+
+// Pointwise kernels of the reference's unit-level functions (exact arithmetic).
+enum PointOp { OP_CONS2PRIM = 0, OP_PRIM2CONS = 1, OP_FLUXES = 2, OP_SPLITTING = 3, OP_BC = 4 };
+cudaError_t launch_pointwise_exact(int op, long long n, const double *a, const double *b, const double *nrm,
+                                   int bc, const double *dir_prim, double *out, double *out2, cudaStream_t s);
+
+} // namespace mmf

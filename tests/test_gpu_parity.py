@@ -1,0 +1,246 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle.
+
+Reference arithmetic ("reference") must be bit-identical to the oracle (which
+is itself bit-identical to the reference sources).  The fast arithmetic must
+stay within 1e-12 relative per cell after the stated step counts: for every
+cell, max_k |U_k - U_ref_k| / max_k |U_ref_k| over the five conserved fields
+(the cell's state error relative to the cell's state).  Per-field ratios are
+not used because fields that are zero up to round-off (the momentum of a
+radial Sod near its axes) have no scale of their own.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FAST_RTOL = 1e-12
+
+
+def rel_err(a, b):
+    """max over cells of the cell-wise relative error (infinity norm over the 5 fields)."""
+    num = np.abs(a - b).max(axis=1)
+    den = np.abs(b).max(axis=1)
+    return float((num / den).max())
+
+
+def oracle_mesh(orc, case, cell_order=0):
+    P = orc.BC_PERIODIC
+    lo = [P] * 3 if case.periodic else None
+    return orc.OracleMesh(case.problem, case.dim, case.n, case.origin, case.length, bc_lo=lo, bc_hi=lo,
+                          cell_order=cell_order)
+
+
+def oracle_params(orc, case):
+    p = case.prm
+    return orc.params(vortex_beta=p.vortex_beta, sod_radius=p.sod_radius, sod_rho_in=p.sod_rho_in,
+                      sod_p_in=p.sod_p_in, sod_rho_out=p.sod_rho_out, sod_p_out=p.sod_p_out,
+                      periodic_exact=int(p.periodic), domain_origin=p.origin, domain_length=p.length)
+
+
+# ---- unit-level functions ---------------------------------------------------------------
+
+def random_states(n, seed, amp=2.0):
+    rng = np.random.default_rng(seed)
+    prim = np.column_stack([rng.uniform(0.05, 3, n), rng.uniform(-amp, amp, (n, 3)), rng.uniform(0.05, 3, n)])
+    return prim
+
+
+def test_pointwise_bitwise(orc, mmf):
+    from minimmerflow_gb300 import euler
+    n = 4096
+    prim = random_states(n, 1)
+    cons = np.array([orc.prim2cons(p) for p in prim])
+    assert np.array_equal(euler.primitive2conservative(prim), cons)
+    assert np.array_equal(euler.conservative2primitive(cons), np.array([orc.cons2prim(c) for c in cons]))
+    rng = np.random.default_rng(2)
+    nrm = rng.normal(size=(n, 3)); nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    p2 = np.array([orc.cons2prim(c) for c in cons])
+    assert np.array_equal(euler.evalFluxes(cons, p2, nrm),
+                          np.array([orc.eval_fluxes(c, p, q) for c, p, q in zip(cons, p2, nrm)]))
+    cr = cons[::-1].copy()
+    F, lam = euler.evalSplitting(cons, cr, nrm)
+    ref = [orc.eval_splitting(a, b, q) for a, b, q in zip(cons, cr, nrm)]
+    assert np.array_equal(F, np.array([r[0] for r in ref]))
+    assert np.array_equal(lam, np.array([r[1] for r in ref]))
+    for bc in (orc.BC_FREE_FLOW, orc.BC_REFLECTING, orc.BC_WALL):
+        g = euler.evalInterfaceBCValues(bc, nrm, cons)
+        assert np.array_equal(g, np.array([orc.eval_bc(0, bc, np.zeros(3), q, c) for c, q in zip(cons, nrm)]))
+    g = euler.evalInterfaceBCValues(orc.BC_DIRICHLET, nrm, cons, [1.0, 3.0, 0.0, 0.0, 1.0 / 1.4])
+    assert np.array_equal(g, np.tile(orc.eval_bc(orc.FFSTEP, orc.BC_DIRICHLET, np.zeros(3), nrm[0], cons[0]),
+                                     (n, 1)))
+
+
+# ---- computeRHS -------------------------------------------------------------------------
+
+RHS_CASES = [("vortex_xy", 2, 64), ("radsod", 2, 64), ("vortex_xy", 3, 16), ("vortex_yz", 3, 16),
+             ("radsod", 3, 16)]
+
+
+@pytest.mark.parametrize("pname,dim,n", RHS_CASES)
+def test_compute_rhs_bitwise(orc, mmf, pname, dim, n):
+    case = mmf.problem.reference_case(pname, dim, n)
+    m = oracle_mesh(orc, case)
+    rng = np.random.default_rng(7)
+    U = m.initial_state() * (1.0 + 0.02 * rng.standard_normal((m.ncells, 1)))
+    R_ref, me_ref = m.compute_rhs(U)
+    with case.solver(arith="reference") as s:
+        R, me = s.compute_rhs(U)
+    assert me == me_ref
+    assert np.array_equal(R, R_ref)
+
+
+@pytest.mark.parametrize("dim,n", [(2, (37, 23, 1)), (2, (1, 9, 1)), (2, (9, 1, 1)), (3, (13, 7, 5)),
+                                   (3, (31, 1, 3)), (3, (61, 14, 9))])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_compute_rhs_ragged_bitwise(orc, mmf, dim, n, periodic):
+    P = mmf.problem
+    case = P.Case("ragged", P.RADSOD, dim, n, (-0.3, -0.2, -0.1), 1.0, 0.5, periodic=periodic,
+                  prm=P.Params(sod_radius=0.3))
+    m = oracle_mesh(orc, case)
+    rng = np.random.default_rng(11)
+    U = m.initial_state(oracle_params(orc, case)) * (1.0 + 0.05 * rng.standard_normal((m.ncells, 1)))
+    R_ref, me_ref = m.compute_rhs(U)
+    with case.solver(arith="reference") as s:
+        R, me = s.compute_rhs(U)
+    assert me == me_ref
+    assert np.array_equal(R, R_ref)
+
+
+def test_compute_rhs_morton_map(orc, mmf):
+    """Raw ids in octree (Morton) order, as bitpit stores VolOctree cells."""
+    case = mmf.problem.reference_case("radsod", 3, 16)
+    m = oracle_mesh(orc, case, cell_order=1)
+    U = m.initial_state()
+    R_ref, me_ref = m.compute_rhs(U)
+    with case.solver(arith="reference") as s:
+        s.set_cell_map(m.grid_of_raw())
+        R, me = s.compute_rhs(U)
+    assert me == me_ref and np.array_equal(R, R_ref)
+
+
+# ---- the time loop ----------------------------------------------------------------------
+
+GOLDEN = ["2dIsentropicVortex", "2dRadSod", "3dIsentropicVortexXY", "3dIsentropicVortexYZ", "3dRadSod"]
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_runs(orc, mmf, name):
+    """Full reference regression runs on the GPU: bit-identical final state with
+    the reference arithmetic, <=1e-12 with the fast one, golden error string."""
+    pname, dim, n, cfl, t_end, golden = orc.GOLDEN_CASES[name]
+    case = mmf.problem.reference_case(pname, dim, n, cfl=cfl, t_end=t_end)
+    m = oracle_mesh(orc, case)
+    U0 = m.initial_state()
+    U_ref, t_ref, steps_ref = m.run(U0, cfl, t_end=t_end)
+    for arith in ("reference", "fast"):
+        with case.solver(arith=arith) as s:
+            U, t, steps = s.run(U0, cfl, t_end=t_end)
+            assert s.status() == 0
+        assert steps == steps_ref
+        err = m.l1_density_error(U, t_end)
+        if arith == "reference":
+            assert t == t_ref
+            assert np.array_equal(U, U_ref)
+            assert "%.12e" % err == golden
+        else:
+            assert abs(t - t_ref) <= 1e-14 * t_ref
+            assert rel_err(U, U_ref) <= FAST_RTOL
+            assert abs(err - float(golden)) <= 1e-10 * float(golden)
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_periodic_vortex_2d_64_100_steps(orc, mmf, arith):
+    """2D vortex 64^2, periodic borders, CFL 0.5, 100 steps (order 1)."""
+    case = mmf.problem.vortex(2, 64, steps=100)
+    m = oracle_mesh(orc, case)
+    prm = oracle_params(orc, case)
+    U0 = m.initial_state(prm)
+    U_ref, t_ref, _ = m.run(U0, case.cfl, max_steps=100)
+    with case.solver(arith=arith) as s:
+        U, t, steps = s.run(U0, case.cfl, max_steps=100)
+    assert steps == 100
+    if arith == "reference":
+        assert np.array_equal(U, U_ref) and t == t_ref
+    else:
+        assert rel_err(U, U_ref) <= FAST_RTOL
+    # periodic borders conserve every field (telescoping face fluxes)
+    np.testing.assert_allclose(U.sum(axis=0), U0.sum(axis=0), rtol=1e-12, atol=1e-10)
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_radial_sod_2d_to_end_time(orc, mmf, arith):
+    """[-1,1]^2 radial Sod (r < 0.5), transmissive borders, CFL 0.5, to t = 0.25 at 128^2."""
+    case = mmf.problem.radial_sod_2d(n=128)
+    m = oracle_mesh(orc, case)
+    U0 = m.initial_state(oracle_params(orc, case))
+    U_ref, t_ref, steps_ref = m.run(U0, case.cfl, t_end=case.t_end)
+    with case.solver(arith=arith) as s:
+        U, t, steps = s.run(U0, case.cfl, t_end=case.t_end)
+    assert steps == steps_ref and abs(t - 0.25) < 1e-15
+    if arith == "reference":
+        assert np.array_equal(U, U_ref)
+    else:
+        assert rel_err(U, U_ref) <= FAST_RTOL
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_vortex_3d_both_axes(orc, mmf, arith):
+    """3D periodic vortex, axis z and axis x, 24^3, 20 steps."""
+    for axis in ("z", "x"):
+        case = mmf.problem.vortex(3, 24, axis=axis, steps=20)
+        m = oracle_mesh(orc, case)
+        U0 = m.initial_state(oracle_params(orc, case))
+        U_ref, t_ref, _ = m.run(U0, case.cfl, max_steps=20)
+        with case.solver(arith=arith) as s:
+            U, t, steps = s.run(U0, case.cfl, max_steps=20)
+        assert steps == 20
+        if arith == "reference":
+            assert np.array_equal(U, U_ref)
+        else:
+            assert rel_err(U, U_ref) <= FAST_RTOL
+
+
+def test_full_size_sod_symmetry_and_mass(mmf):
+    """1024^2 radial Sod, a few steps: the solution keeps the x<->y and mirror
+    symmetries of the initial state, and mass is conserved while the waves are
+    inside the domain."""
+    case = mmf.problem.radial_sod_2d(n=1024)
+    U0 = case.initial_state()
+    with case.solver(arith="fast") as s:
+        U, t, steps = s.run(U0, case.cfl, max_steps=20)
+    assert steps == 20
+    rho = U[:, 0].reshape(1024, 1024)
+    np.testing.assert_allclose(rho, rho.T, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(rho, rho[::-1, :], rtol=1e-13, atol=0)
+    assert abs(U[:, 0].sum() - U0[:, 0].sum()) <= 1e-12 * U0[:, 0].sum()
+
+
+def test_end_time_and_step_limit(orc, mmf):
+    case = mmf.problem.reference_case("radsod", 2, 32, t_end=0.3)
+    U0 = case.initial_state()
+    with case.solver(arith="reference") as s:
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, 0.3, -1)
+        t, done = s.advance(1000)
+        assert t == 0.3
+        t2, done2 = s.advance(5)   # past the end time: nothing runs
+        assert done2 == 0 and t2 == 0.3
+        s.time_setup(case.cfl, 0.0, math.inf, 7)
+        t3, done3 = s.advance(100)
+        assert done3 == 7
+
+
+def test_status_reports_negative_pressure(mmf):
+    """A non-physical input state (negative pressure) is reported, not trapped."""
+    case = mmf.problem.reference_case("radsod", 2, 16)
+    U0 = case.initial_state()
+    U0[5, 4] = -1.0   # rho E < 0
+    with case.solver(arith="fast") as s:
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, math.inf, 1)
+        with pytest.raises(mmf.capi.MMFError) as ei:
+            s.advance(1)
+        assert ei.value.code == mmf.capi.MMF_ERR_STATE
+        assert s.status() & 2
