@@ -37,12 +37,13 @@ FP64_OPS_PER_CELL_STAGE = None  # filled from the kernel model below (fast arith
 
 
 def fp64_ops_per_cell_update_2d():
-    """FP64 instructions per cell-update of the fast 2D kernel (per-cell model):
-    record: 1/rho (division, ~9 DFMA-equivalent), 3 mul (u,v,w), 2 fma + 1 mul (rho|u|^2),
-    2 (p), 2 + sqrt (~10) (a), 1 (E+p), fluxes 2 dirs x 5, 1 shared mul  -> ~41
-    faces: 2 per cell x (5 x (add, sub, fma) + max) = 32; accumulate 5 x 3 = 15;
-    stage update ~(5 stage1: 0, stage2: 5 fma load + 15, stage3: 15)/3 avg ~ 12."""
-    return 3 * (41 + 32 + 15) + 35
+    """FP64 instructions per cell-update of the fast 2D kernel with zero
+    z-momentum (four stored fields), counted from the source per cell and stage:
+    record 29 (Newton reciprocal 4 + MUFU, velocities 2, rho|u|^2 2, p 2, a 9 with
+    MUFU, E+p 1, fluxes 5, wave speeds 2, status 0), faces 2 x 12, accumulation 12,
+    stage update (0, 8, 12) and the stage-2 state (4)  ->  65 + (0, 12, 12) per stage,
+    plus 1/16 for the two halo lanes of a warp."""
+    return int(round((3 * 65 + 24) * 32 / 30))
 
 
 def read_peaks():
@@ -167,30 +168,53 @@ def cpu_baseline(n, seconds, procs):
 
 
 # ---------------------------------------------------------------- GPU arm
+def make_case(args):
+    import minimmerflow_gb300 as mmf
+    if args.workload == "sod2d":
+        return mmf.problem.radial_sod_2d(n=args.n)
+    axis = "z" if args.workload == "vortex3d_z" else "x"
+    case = mmf.problem.vortex(3, args.n, axis=axis, steps=50)
+    case.t_end = math.inf
+    return case
+
+
+def workload_config(args, world):
+    if args.workload == "sod2d":
+        w = "2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, to t=0.25, order 1, FP64" % (args.n, args.n)
+        cells = args.n * args.n
+    else:
+        w = ("3D isentropic vortex %d^3, [-5,5]^3, periodic, beta=5, axis %s, CFL 0.5, 50-step runs, order 1, FP64"
+             % (args.n, args.workload[-1]))
+        cells = args.n ** 3
+    return {"workload": w, "cells": cells, "l2": "flushed between timed steps (512 MB write)",
+            "parallelism": "replicas x%d" % world}
+
+
 def run_ours(args, world, rank, local, dist):
     import numpy as np
     import torch
     import minimmerflow_gb300 as mmf
 
     torch.cuda.set_device(local)
-    case = mmf.problem.radial_sod_2d(n=args.n)
+    case = make_case(args)
     U0 = case.initial_state()
     ncell = case.ncells
     s = case.solver(arith=args.arith, device=local, chunk=args.chunk)
     stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    limit = case.max_steps if math.isinf(case.t_end) else -1
+
     def restart():
         s.upload(U0)
-        s.time_setup(case.cfl, 0.0, case.t_end, -1)
+        s.time_setup(case.cfl, 0.0, case.t_end, limit)
 
     restart()
     steps_done = 0
 
     def ensure_room():
-        nonlocal steps_done
         t, st = s.time_info()
-        if t >= case.t_end - 1e-15:
+        if t >= case.t_end - 1e-15 or (limit >= 0 and st >= limit):
             restart()
 
     # warm-up
@@ -202,10 +226,8 @@ def run_ours(args, world, rank, local, dist):
     def timed_steps(k):
         """k steps, each bracketed by events on the library stream; L2 flushed between."""
         durs = []
-        check_every = 16
         for i in range(k):
-            if i % check_every == 0:
-                ensure_room()
+            ensure_room()
             flush.zero_()
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -238,8 +260,7 @@ def run_ours(args, world, rank, local, dist):
     # per-stage launch times (stage 2 = dominant kernel, roofline)
     stage_t = {1: [], 2: [], 3: []}
     for i in range(max(8, min(args.steps, 64))):
-        if i % 16 == 0:
-            ensure_room()
+        ensure_room()
         flush.zero_()
         torch.cuda.synchronize()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -257,12 +278,12 @@ def run_ours(args, world, rank, local, dist):
     host = torch.empty((ncell, 5), dtype=torch.float64, pin_memory=True)
     hv = host.numpy()
     hv[:] = U0
-    s.time_setup(case.cfl, 0.0, case.t_end, -1)
-    k_e2e = max(3, min(args.steps, 50))
+    s.time_setup(case.cfl, 0.0, case.t_end, limit)
+    k_e2e = max(3, min(args.steps, 50 if case.ncells < 4e6 else 10))
     for _ in range(2):
         s.advance_host(hv, 1)
     hv[:] = U0
-    s.time_setup(case.cfl, 0.0, case.t_end, -1)
+    s.time_setup(case.cfl, 0.0, case.t_end, -1 if limit < 0 else 10 ** 9)
     t0 = time.perf_counter()
     for _ in range(k_e2e):
         s.advance_host(hv, 1)
@@ -280,16 +301,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
-    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--workload", default="sod2d", choices=["sod2d", "vortex3d_z", "vortex3d_x"])
+    ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    if args.n <= 0:
+        args.n = 1024 if args.workload == "sod2d" else 256
     world, rank, local, dist = dist_setup(args)
-    workload = {"workload": "2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, to t=0.25, order 1, FP64" % (args.n, args.n),
-                "cells": args.n * args.n, "l2": "flushed between timed steps (512 MB write)",
-                "parallelism": "replicas x%d" % world}
+    workload = workload_config(args, world)
     metric = "cell-updates/s"
 
     if args.impl == "reference":
@@ -319,28 +341,29 @@ def main():
     traffic = None
     if traffic_rec and str(args.n) in traffic_rec.get("per_launch_bytes", {}):
         traffic = traffic_rec["per_launch_bytes"][str(args.n)].get("stage%d" % dom)
-    fp64_ops = fp64_ops_per_cell_update_2d()
+    fp64_ops = fp64_ops_per_cell_update_2d() if args.workload == "sod2d" else None
     fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock)
     line = {
         "metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload,
         "arith": args.arith,
-        "roofline": {"bound": "hbm", "kernel": "stage%d (stage2d_kernel<%s>)" % (dom, args.arith),
+        "roofline": {"bound": "hbm", "kernel": "stage%d (stage%dd_kernel<%s>)" % (dom, r["case"].dim, args.arith),
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "peak_source": peak_src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": STAGE_BYTES[dom] * ncell,
                      "stage_ms": {str(k): 1e3 * v for k, v in r["st_mean"].items()}},
         "fp64": {"ops_per_cell_update_model": fp64_ops,
-                 "achieved_ops_per_s": fp64_ops * r["value"] / world,
-                 "peak_ops_per_s": fp64_peak, "frac": fp64_ops * r["value"] / world / fp64_peak,
+                 "achieved_ops_per_s": fp64_ops * r["value"] / world if fp64_ops else None,
+                 "peak_ops_per_s": fp64_peak,
+                 "frac": fp64_ops * r["value"] / world / fp64_peak if fp64_ops else None,
                  "peak_source": "measured DFMA issue rate (probe), not in MEASURED_PEAKS.json"},
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],
         "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,
                 "d2h_bytes_per_step": 40 * ncell},
     }
-    if not args.no_cpu:
+    if not args.no_cpu and args.workload == "sod2d":
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
     print(json.dumps(line))
 

@@ -140,6 +140,11 @@ int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, co
 int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
                        const double *dirichlet_prim, double *cons_bc);
 
+/* Self-test of the reciprocal and square root of MMF_ARITH_FAST (Newton
+ * iterations on the hardware approximations): rcp[i] ~ 1/x[i], sqrt[i] ~ sqrt(x[i])
+ * for positive x.  No reference counterpart; used to check the error bound. */
+int mmf_newton_selftest(int64_t n, const double *x, double *rcp, double *sqrt_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,15 @@ __global__ void aos_to_soa_kernel(const double *__restrict__ aos, double *__rest
     for (int k = 0; k < NF; ++k) soa[k * plane + g] = aos[NF * r + k];
 }
 
+// flag := 1 if any value of the plane is not +0.0 / -0.0
+__global__ void nonzero_plane_kernel(const double *__restrict__ v, long long n, int *flag)
+{
+    bool nz = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        nz |= (__double_as_longlong(v[i]) << 1) != 0;
+    if (__any_sync(0xffffffffu, nz) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__restrict__ aos, long long n_raw,
                                   long long plane, const long long *__restrict__ raw_to_cell)
 {
@@ -73,6 +82,8 @@ struct mmf_ctx {
     long long launches = 0;
     double cfl = 0.0;
     bool time_ready = false;
+    bool w_zero = false;      // 2D state with identically zero z-momentum
+    int *flag = nullptr;      // device scratch flag
 
     cudaError_t stage(int st, const double *U_in, double *out)
     {
@@ -84,7 +95,7 @@ struct mmf_ctx {
         sa.ctrl = ctrl;
         sa.rhs_maxeig = rhs_maxeig;
         ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_stage_fast(st, gp, sa, stream)
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_stage_fast(st, gp, sa, stream, w_zero)
                                                                 : launch_stage_exact(st, gp, sa, stream);
     }
     cudaError_t rk_step()
@@ -162,6 +173,7 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     if (e == cudaSuccess) e = cudaMalloc(&c->aos, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->ctrl, sizeof(Ctrl));
     if (e == cudaSuccess) e = cudaMalloc(&c->rhs_maxeig, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(c->U, 0, bytes, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->ctrl, 0, sizeof(Ctrl), c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -182,7 +194,7 @@ int mmf_destroy(mmf_ctx *c)
     if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
     if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
-    cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig);
+    cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MMF_OK;
@@ -221,6 +233,31 @@ static int to_soa(mmf_ctx *c, const double *d_aos, double *soa, int64_t n_raw)
     return MMF_OK;
 }
 
+// After a state upload: choose the 2D kernels without z-momentum when that
+// plane is identically zero (the graphs are rebuilt when the choice changes).
+static int refresh_w_zero(mmf_ctx *c)
+{
+    bool wz = false;
+    if (c->gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST) {
+        MMF_CUDA(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
+        const long long n = c->gp.plane;
+        const unsigned blocks = (unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+        nonzero_plane_kernel<<<blocks, 256, 0, c->stream>>>(c->U + 3 * n, n, c->flag);
+        ++c->launches;
+        MMF_CUDA(cudaPeekAtLastError());
+        int h = 1;
+        MMF_CUDA(cudaMemcpyAsync(&h, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        MMF_CUDA(cudaStreamSynchronize(c->stream));
+        wz = (h == 0);
+    }
+    if (wz != c->w_zero) {
+        if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+        if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
+        c->w_zero = wz;
+    }
+    return MMF_OK;
+}
+
 static int from_soa(mmf_ctx *c, const double *soa, double *d_aos, int64_t n_raw)
 {
     const unsigned blocks = (unsigned)((n_raw + 255) / 256);
@@ -236,7 +273,8 @@ int mmf_upload_state(mmf_ctx *c, const double *aos, int64_t n_raw)
     if (rc) return rc;
     if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
     MMF_CUDA(cudaMemcpyAsync(c->aos, aos, sizeof(double) * NF * n_raw, cudaMemcpyHostToDevice, c->stream));
-    return to_soa(c, c->aos, c->U, n_raw);
+    if ((rc = to_soa(c, c->aos, c->U, n_raw))) return rc;
+    return refresh_w_zero(c);
 }
 
 int mmf_download_state(mmf_ctx *c, double *aos, int64_t n_raw)
@@ -255,7 +293,8 @@ int mmf_upload_state_device(mmf_ctx *c, const double *d_aos, int64_t n_raw)
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!d_aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
-    return to_soa(c, d_aos, c->U, n_raw);
+    if ((rc = to_soa(c, d_aos, c->U, n_raw))) return rc;
+    return refresh_w_zero(c);
 }
 
 int mmf_download_state_device(mmf_ctx *c, double *d_aos, int64_t n_raw)
@@ -528,6 +567,26 @@ int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const doubl
         return fail(MMF_ERR_ARG, "unknown border condition");
     if (bc_type == MMF_BC_DIRICHLET && !dirichlet_prim) return fail(MMF_ERR_ARG, "Dirichlet needs a state");
     return pointwise(OP_BC, n, cons, nullptr, normal, bc_type, dirichlet_prim, cons_bc, nullptr);
+}
+
+int mmf_newton_selftest(int64_t n, const double *x, double *rcp, double *sqrt_out)
+{
+    if (!x || !rcp || !sqrt_out || n < 0) return fail(MMF_ERR_ARG, "bad buffers");
+    if (n == 0) return MMF_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(MMF_ERR_CUDA, "no CUDA device available");
+    const size_t b = sizeof(double) * (size_t)n;
+    double *dx = nullptr, *dr = nullptr, *dq = nullptr;
+    cudaError_t e = cudaMalloc(&dx, b);
+    if (e == cudaSuccess) e = cudaMalloc(&dr, b);
+    if (e == cudaSuccess) e = cudaMalloc(&dq, b);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_newton_selftest(n, dx, dr, dq, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(rcp, dr, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(sqrt_out, dq, b, cudaMemcpyDeviceToHost);
+    cudaFree(dx); cudaFree(dr); cudaFree(dq);
+    if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
+    return MMF_OK;
 }
 
 } // extern "C"

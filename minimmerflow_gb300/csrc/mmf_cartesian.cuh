@@ -72,6 +72,9 @@ enum { STAGE_RHS = 0, STAGE_1 = 1, STAGE_2 = 2, STAGE_3 = 3 };
 template <class A> struct IsExact { static constexpr bool value = false; };
 template <> struct IsExact<ExactArith> { static constexpr bool value = true; };
 
+template <class A, int DIM>
+using RecOf = CellRecV<DIM, A::NVAR>;
+
 __device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
 __device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
 
@@ -138,8 +141,8 @@ __device__ __forceinline__ void load_state(const StageArgs &sa, const GridParams
                                            long long g, double *c)
 {
 #pragma unroll
-    for (int k = 0; k < NF; ++k) {
-        const long long o = (long long)k * gp.plane + g;
+    for (int k = 0; k < A::NVAR; ++k) {
+        const long long o = (long long)A::field(k) * gp.plane + g;
         if (STAGE == STAGE_2) {
             const double u = __ldg(sa.U + o), r = __ldg(sa.R + o);
             if (IsExact<A>::value) c[k] = u + sc.dt * r / gp.vol;   // main.cpp:421
@@ -153,20 +156,22 @@ __device__ __forceinline__ void load_state(const StageArgs &sa, const GridParams
 }
 
 // Stage output of grid cell g from its residual accumulator and stage state.
+// Fast stage 2 uses W2 = 3/4 U + 1/4 (W1 + s R2) = U + s/4 (R1 + R2), which
+// is the same combination with W1 = U + s R1 substituted.
 template <class A, int STAGE>
 __device__ __forceinline__ void store_output(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
                                              long long g, const double *acc, const double *cstate)
 {
 #pragma unroll
-    for (int k = 0; k < NF; ++k) {
-        const long long o = (long long)k * gp.plane + g;
+    for (int k = 0; k < A::NVAR; ++k) {
+        const long long o = (long long)A::field(k) * gp.plane + g;
         double v;
         if (STAGE == STAGE_RHS || STAGE == STAGE_1) {
             v = acc[k];
         } else if (STAGE == STAGE_2) {
             const double u = __ldg(sa.U + o);
             if (IsExact<A>::value) v = 0.75 * u + 0.25 * (cstate[k] + sc.dt * acc[k] / gp.vol); // main.cpp:457
-            else v = fma(0.25, fma(sc.s, acc[k], cstate[k]), 0.75 * u);
+            else v = fma(0.25 * sc.s, __ldg(sa.R + o) + acc[k], u);
         } else {
             const double u = sa.out[o];   // in place: U
             if (IsExact<A>::value) v = (1. / 3) * u + (2. / 3) * (cstate[k] + sc.dt * acc[k] / gp.vol); // main.cpp:493
@@ -182,7 +187,7 @@ __device__ __forceinline__ void accumulate_pair(double *acc, const double *Flo, 
                                                 bool hi_first)
 {
 #pragma unroll
-    for (int k = 0; k < NF; ++k) {
+    for (int k = 0; k < A::NVAR; ++k) {
         if (IsExact<A>::value) {
             if (hi_first) { acc[k] = acc[k] - area * Fhi[k]; acc[k] = acc[k] + area * Flo[k]; }
             else { acc[k] = acc[k] + area * Flo[k]; acc[k] = acc[k] - area * Fhi[k]; }
@@ -213,7 +218,7 @@ __device__ __forceinline__ int resolve_index(int i, int n, bool periodic, int &g
 // Record of the cell at (x, y, z) (may be a ghost) for this stage.
 template <class A, int STAGE, int DIM>
 __device__ __forceinline__ void load_record(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
-                                            int x, int y, int z, CellRec<DIM> &r, unsigned *status)
+                                            int x, int y, int z, RecOf<A, DIM> &r, unsigned *status)
 {
     int gx, gy, gz = 0;
     const int ix = resolve_index(x, gp.n[0], gp.bc_lo[0] == BC_PERIODIC, gx);
@@ -225,24 +230,24 @@ __device__ __forceinline__ void load_record(const StageArgs &sa, const GridParam
     if (ghost) {
         if (gx) {
             const double n[3] = {(double)gx, 0.0, 0.0};
-            double t[NF];
+            double t[A::NVAR];
             ghost_state<A>(gx < 0 ? gp.bc_lo[0] : gp.bc_hi[0], n, r.c, gp.dir_prim, t);
 #pragma unroll
-            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
         }
         if (gy) {
             const double n[3] = {0.0, (double)gy, 0.0};
-            double t[NF];
+            double t[A::NVAR];
             ghost_state<A>(gy < 0 ? gp.bc_lo[1] : gp.bc_hi[1], n, r.c, gp.dir_prim, t);
 #pragma unroll
-            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
         }
         if (DIM == 3 && gz) {
             const double n[3] = {0.0, 0.0, (double)gz};
-            double t[NF];
+            double t[A::NVAR];
             ghost_state<A>(gz < 0 ? gp.bc_lo[2] : gp.bc_hi[2], n, r.c, gp.dir_prim, t);
 #pragma unroll
-            for (int k = 0; k < NF; ++k) r.c[k] = t[k];
+            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
         }
     }
     A::template record<DIM>(r, ghost ? nullptr : status);
@@ -250,22 +255,23 @@ __device__ __forceinline__ void load_record(const StageArgs &sa, const GridParam
 
 // Face between record L (this lane) and record R along direction d.
 template <class A, int DIM>
-__device__ __forceinline__ double face_dir(const CellRec<DIM> &L, const CellRec<DIM> &R, int d, double *F)
+__device__ __forceinline__ double face_dir(const RecOf<A, DIM> &L, const RecOf<A, DIM> &R, int d, double *F)
 {
     return A::face(L.c, L.f[d], L.lam[d], R.c, R.f[d], R.lam[d], F);
 }
 
 // x-faces of a warp row: Fhi = face(lane, lane+1), Flo = face(lane-1, lane).
 template <class A, int DIM>
-__device__ __forceinline__ double xfaces(const CellRec<DIM> &r, double *Flo, double *Fhi)
+__device__ __forceinline__ double xfaces(const RecOf<A, DIM> &r, double *Flo, double *Fhi)
 {
-    double cR[NF], fR[NF];
+    constexpr int NV = A::NVAR;
+    double cR[NV], fR[NV];
 #pragma unroll
-    for (int k = 0; k < NF; ++k) { cR[k] = shfl_down(r.c[k], 1); fR[k] = shfl_down(r.f[0][k], 1); }
+    for (int k = 0; k < NV; ++k) { cR[k] = shfl_down(r.c[k], 1); fR[k] = shfl_down(r.f[0][k], 1); }
     const double lamR = shfl_down(r.lam[0], 1);
     const double lam = A::face(r.c, r.f[0], r.lam[0], cR, fR, lamR, Fhi);
 #pragma unroll
-    for (int k = 0; k < NF; ++k) Flo[k] = shfl_up(Fhi[k], 1);
+    for (int k = 0; k < NV; ++k) Flo[k] = shfl_up(Fhi[k], 1);
     return lam;
 }
 
@@ -292,32 +298,33 @@ __global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs s
     unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
     double lmax = 0.0;
 
-    CellRec<2> cur, abv;
-    double Fylo[NF], Fyhi[NF], Fxlo[NF], Fxhi[NF], acc[NF];
+    constexpr int NV = A::NVAR;
+    RecOf<A, 2> cur, abv;
+    double Fylo[NV], Fyhi[NV], Fxlo[NV], Fxhi[NV], acc[NV];
     load_record<A, STAGE, 2>(sa, gp, sc, x, y0 - 1, 0, abv, nullptr);
     load_record<A, STAGE, 2>(sa, gp, sc, x, y0, 0, cur, st);
     {
         const double l = face_dir<A, 2>(abv, cur, 1, Fylo);
-        if (out_col) lmax = fmax(lmax, l);
+        if (out_col) lmax = max_nonneg(lmax, l);
     }
     for (int y = y0; y < y1; ++y) {
         load_record<A, STAGE, 2>(sa, gp, sc, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
         const double ly = face_dir<A, 2>(cur, abv, 1, Fyhi);
         const double lx = xfaces<A, 2>(cur, Fxlo, Fxhi);
         if (STAGE <= STAGE_1) {
-            if (out_col) lmax = fmax(lmax, ly);
-            if (xface_valid) lmax = fmax(lmax, lx);
+            if (out_col) lmax = max_nonneg(lmax, ly);
+            if (xface_valid) lmax = max_nonneg(lmax, lx);
         }
         if (out_col) {
 #pragma unroll
-            for (int k = 0; k < NF; ++k) acc[k] = 0.0;
+            for (int k = 0; k < NV; ++k) acc[k] = 0.0;
             accumulate_pair<A>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
             accumulate_pair<A>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
             store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * y, acc, cur.c);
         }
         cur = abv;
 #pragma unroll
-        for (int k = 0; k < NF; ++k) Fylo[k] = Fyhi[k];
+        for (int k = 0; k < NV; ++k) Fylo[k] = Fyhi[k];
     }
     if (STAGE <= STAGE_1) {
         lmax = warp_max(lmax);
@@ -372,7 +379,7 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
     unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
     double lmax = 0.0;
 
-    CellRec<3> cur, abv;
+    RecOf<A, 3> cur, abv;
     double Fzlo[NF], Fzhi[NF], Fxlo[NF], Fxhi[NF], Fylo[NF], Fyhi[NF], acc[NF];
     load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, abv, nullptr);
     load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);

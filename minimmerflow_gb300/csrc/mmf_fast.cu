@@ -4,9 +4,25 @@
 
 namespace mmf {
 
-cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s)
+cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s, bool w_zero)
 {
+    if (gp.dim == 2 && w_zero) return launch_stage<FastArith2DW0, false>(stage, gp, sa, s);
     return launch_stage<FastArith>(stage, gp, sa, s);
+}
+
+__global__ void newton_selftest_kernel(long long n, const double *x, double *r, double *q)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r[i] = rcp_newton(x[i]);
+    q[i] = sqrt_newton(x[i]);
+}
+
+cudaError_t launch_newton_selftest(long long n, const double *x, double *r, double *q, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    newton_selftest_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, x, r, q);
+    return cudaPeekAtLastError();
 }
 
 } // namespace mmf

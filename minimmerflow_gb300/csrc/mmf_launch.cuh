@@ -38,30 +38,38 @@ inline long long cartesian_blocks(const GridParams &gp)
     return (long long)gp.nseg * gp.nrowblk * gp.nchunk;
 }
 
-template <class A, int STAGE>
+template <class A, int STAGE, bool HAS3D>
 inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cudaStream_t s)
 {
     const unsigned blocks = (unsigned)cartesian_blocks(gp);
-    if (gp.dim == 2) stage2d_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa);
-    else stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
+    if (gp.dim == 2) {
+        stage2d_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa);
+    } else {
+        if constexpr (HAS3D) stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
+        else return cudaErrorInvalidValue;
+    }
     return cudaPeekAtLastError();
 }
 
-template <class A>
+template <class A, bool HAS3D = true>
 inline cudaError_t launch_stage(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s)
 {
     switch (stage) {
-    case STAGE_RHS: return launch_stage_t<A, STAGE_RHS>(gp, sa, s);
-    case STAGE_1: return launch_stage_t<A, STAGE_1>(gp, sa, s);
-    case STAGE_2: return launch_stage_t<A, STAGE_2>(gp, sa, s);
-    case STAGE_3: return launch_stage_t<A, STAGE_3>(gp, sa, s);
+    case STAGE_RHS: return launch_stage_t<A, STAGE_RHS, HAS3D>(gp, sa, s);
+    case STAGE_1: return launch_stage_t<A, STAGE_1, HAS3D>(gp, sa, s);
+    case STAGE_2: return launch_stage_t<A, STAGE_2, HAS3D>(gp, sa, s);
+    case STAGE_3: return launch_stage_t<A, STAGE_3, HAS3D>(gp, sa, s);
     default: return cudaErrorInvalidValue;
     }
 }
 
-// Entry points of the two arithmetic translation units.
+// Entry points of the two arithmetic translation units.  w_zero selects the
+// 2D kernels that skip the identically-zero z-momentum.
 cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
-cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
+cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s, bool w_zero);
+
+// Reciprocal and square root of the fast arithmetic, for the self-test.
+cudaError_t launch_newton_selftest(long long n, const double *x, double *r, double *q, cudaStream_t s);
 
 // Pointwise kernels of the reference's unit-level functions (exact arithmetic).
 enum PointOp { OP_CONS2PRIM = 0, OP_PRIM2CONS = 1, OP_FLUXES = 2, OP_SPLITTING = 3, OP_BC = 4 };

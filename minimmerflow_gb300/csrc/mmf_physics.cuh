@@ -29,14 +29,19 @@ enum BCType : int { BC_NONE = -1, BC_FREE_FLOW = 0, BC_REFLECTING = 1, BC_WALL =
 
 // Cell record: the state and what the faces of the cell need from it.
 // f[d][k] is the physical flux along +e_d, lam[d] the wave speed |u_d| + a.
-template <int DIM>
-struct CellRec {
-    double c[NF];
-    double f[DIM][NF];
+template <int DIM, int NV>
+struct CellRecV {
+    double c[NV];
+    double f[DIM][NV];
     double lam[DIM];
 };
+template <int DIM>
+using CellRec = CellRecV<DIM, NF>;
 
 struct ExactArith {
+    static constexpr int NVAR = NF;
+    __host__ __device__ static constexpr int field(int k) { return k; }
+    __device__ __forceinline__ static void dirichlet(const double *dir_prim, double *g);
     // utils.cpp:48-63
     __device__ __forceinline__ static void cons2prim(const double *c, double *p)
     {
@@ -122,58 +127,134 @@ struct ExactArith {
     }
 };
 
-struct FastArith {
-    // Same record in the fast formulation: u = m / rho with one division,
-    // p = (gamma-1)(E - m.u/2), a = sqrt(gamma p / rho), flux from m and E+p.
+// Reciprocal by the Newton-Raphson iteration y <- y + y (1 - x y), seeded
+// with the hardware reciprocal approximation of the high word
+// (rcp.approx.ftz.f64); two iterations square the seed error twice.
+// For positive normal x (densities); checked against IEEE division in the
+// GPU tests.
+__device__ __forceinline__ double rcp_newton(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+// Square root by the coupled Newton iteration on s ~ sqrt(x) and
+// r ~ 1/(2 sqrt(x)) (Goldschmidt's form), seeded with rsqrt.approx.ftz.f64,
+// followed by one Newton correction s <- s + r (x - s^2).  x >= 0; x = 0
+// returns 0 (selected on the bit pattern, no FP64 compare).
+__device__ __forceinline__ double sqrt_newton(double x)
+{
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double s = x * y;
+    double r = 0.5 * y;
+    const double e = fma(-s, r, 0.5);
+    s = fma(s, e, s);
+    r = fma(r, e, r);
+    const double d = fma(-s, s, x);
+    s = fma(d, r, s);
+    return (__double_as_longlong(x) == 0ll) ? 0.0 : s;
+}
+
+// max of two non-negative doubles through their bit patterns (integer pipe)
+__device__ __forceinline__ double max_nonneg(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    return __longlong_as_double(ia > ib ? ia : ib);
+}
+
+// status bits from the sign / exponent bits (integer pipe): rho < 0, p < 0, NaN
+__device__ __forceinline__ unsigned state_flags(double rho, double p)
+{
+    const long long ir = __double_as_longlong(rho), ip = __double_as_longlong(p);
+    unsigned f = 0;
+    if (ir < 0) f |= 1u;
+    if (ip < 0) f |= 2u;
+    if (((ir >> 52) & 0x7ff) == 0x7ff || ((ip >> 52) & 0x7ff) == 0x7ff) f |= 4u;
+    return f;
+}
+
+// Fast arithmetic.  NV = number of stored fields: 5 = (rho, mx, my, mz, E);
+// 4 = (rho, mx, my, E) for 2D states whose z-momentum is identically zero
+// (the reference keeps it exactly +0 in 2D, problem.cpp:319-323), which
+// removes a fifth of the work.
+template <int NV>
+struct FastArithT {
+    static constexpr int NVAR = NV;
+    static constexpr int IE = NV - 1;   // index of rho E in the stored fields
+
+    // physical field plane of stored field k
+    __host__ __device__ static constexpr int field(int k) { return (NV == 4 && k == 3) ? 4 : k; }
+
     template <int DIM>
-    __device__ __forceinline__ static void record(CellRec<DIM> &r, unsigned *status)
+    __device__ __forceinline__ static void record(CellRecV<DIM, NV> &r, unsigned *status)
     {
         const double rho = r.c[0];
-        const double rinv = 1.0 / rho;
-        const double u = r.c[1] * rinv, v = r.c[2] * rinv, w = r.c[3] * rinv;
-        const double q = fma(r.c[3], w, fma(r.c[2], v, r.c[1] * u));       // rho |u|^2
-        const double p = (GAMMA - 1.0) * fma(-0.5, q, r.c[4]);
-        if (status) {
-            if (rho < 0.0) *status |= 1u;
-            if (p < 0.0) *status |= 2u;
-            if (rho != rho || p != p) *status |= 4u;
-        }
-        const double a = sqrt(GAMMA * p * rinv);
-        const double H = r.c[4] + p;                                    // rho * total enthalpy
+        const double rinv = rcp_newton(rho);
+        const double u = r.c[1] * rinv, v = r.c[2] * rinv;
+        const double w = (NV == 5) ? r.c[3] * rinv : 0.0;
+        double q = fma(r.c[2], v, r.c[1] * u);              // rho |u|^2
+        if (NV == 5) q = fma(r.c[3], w, q);
+        const double E = r.c[IE];
+        const double p = fma(-0.5 * (GAMMA - 1.0), q, (GAMMA - 1.0) * E);
+        if (status) *status |= state_flags(rho, p);
+        const double a = sqrt_newton(GAMMA * p * rinv);
+        const double H = E + p;                             // rho * total enthalpy
+        const double muv = r.c[1] * v;                      // rho u v
         const double vel[3] = {u, v, w};
-        const double muv = r.c[1] * v;                                  // rho u v, shared by f_x[2], f_y[1]
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
             const double m = r.c[1 + d];
             r.f[d][0] = m;
             r.f[d][1] = (d == 0) ? fma(m, u, p) : (d == 1 ? muv : m * u);
             r.f[d][2] = (d == 1) ? fma(m, v, p) : (d == 0 ? muv : m * v);
-            r.f[d][3] = (d == 2) ? fma(m, w, p) : m * w;
-            r.f[d][4] = vel[d] * H;
+            if (NV == 5) r.f[d][3] = (d == 2) ? fma(m, w, p) : m * w;
+            r.f[d][IE] = vel[d] * H;
             r.lam[d] = fabs(vel[d]) + a;
         }
     }
-    // G = (f_L + f_R) - lambda (U_R - U_L): the face flux times 2 (the 1/2 and
-    // the area are applied in the stage update).
+    // G = (f_L + f_R) - lambda (U_R - U_L): twice the face flux (the 1/2 and the
+    // area are applied in the stage update).
     __device__ __forceinline__ static double face(const double *cL, const double *fL, double lamL,
                                                   const double *cR, const double *fR, double lamR, double *G)
     {
-        double lambda = fmax(lamL, lamR);
+        const double lambda = max_nonneg(lamL, lamR);
 #pragma unroll
-        for (int k = 0; k < NF; ++k) G[k] = fma(-lambda, cR[k] - cL[k], fL[k] + fR[k]);
+        for (int k = 0; k < NV; ++k) G[k] = fma(-lambda, cR[k] - cL[k], fL[k] + fR[k]);
         return lambda;
     }
+    // mirror the normal momentum; rho and E are unchanged
     __device__ __forceinline__ static void reflect(const double *n, const double *c, double *cbc)
     {
-        // mirror the normal momentum: rho and E are unchanged
-        const double mn = c[1] * n[0] + c[2] * n[1] + c[3] * n[2];
+        double mn = c[1] * n[0] + c[2] * n[1];
+        if (NV == 5) mn = fma(c[3], n[2], mn);
         cbc[0] = c[0];
         cbc[1] = fma(-2.0 * mn, n[0], c[1]);
         cbc[2] = fma(-2.0 * mn, n[1], c[2]);
-        cbc[3] = fma(-2.0 * mn, n[2], c[3]);
-        cbc[4] = c[4];
+        if (NV == 5) cbc[3] = fma(-2.0 * mn, n[2], c[3]);
+        cbc[IE] = c[IE];
+    }
+    // Dirichlet ghost (utils.cpp:71-83 of the inflow primitive state)
+    __device__ __forceinline__ static void dirichlet(const double *dir_prim, double *g)
+    {
+        double c[NF];
+        ExactArith::prim2cons(dir_prim, c);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) g[k] = c[field(k)];
     }
 };
+
+using FastArith = FastArithT<5>;
+using FastArith2DW0 = FastArithT<4>;
+
+__device__ __forceinline__ void ExactArith::dirichlet(const double *dir_prim, double *g)
+{
+    prim2cons(dir_prim, g);   // euler.cpp:366-376
+}
 
 // Ghost state behind a border face (euler.cpp:261-308, 347-376).  'n' is the
 // outward normal of the border face; dir_prim is the Dirichlet primitive state.
@@ -184,10 +265,10 @@ __device__ __forceinline__ void ghost_state(int bc, const double *n, const doubl
     if (bc == BC_REFLECTING || bc == BC_WALL) {
         A::reflect(n, c, g);
     } else if (bc == BC_DIRICHLET) {
-        ExactArith::prim2cons(dir_prim, g);
+        A::dirichlet(dir_prim, g);
     } else {
 #pragma unroll
-        for (int k = 0; k < NF; ++k) g[k] = c[k];
+        for (int k = 0; k < A::NVAR; ++k) g[k] = c[k];
     }
 }
 

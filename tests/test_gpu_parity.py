@@ -72,6 +72,40 @@ def test_pointwise_bitwise(orc, mmf):
                                      (n, 1)))
 
 
+def test_newton_reciprocal_and_sqrt_error_bound(mmf):
+    """The fast arithmetic's reciprocal and square root (Newton iterations on the
+    hardware approximations) are within 1 ulp of the correctly rounded values."""
+    lib = mmf.capi.load()
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.uniform(1e-3, 1e3, 200000), 10.0 ** rng.uniform(-30, 30, 50000),
+                        np.array([1.0, 2.0, 0.125, 0.1, 1.4, 7.0])])
+    r = np.empty_like(x); q = np.empty_like(x)
+    mmf.capi.check(lib.mmf_newton_selftest(x.size, mmf.capi.ptr(x), mmf.capi.ptr(r), mmf.capi.ptr(q)))
+    ulp_r = np.abs(r - 1.0 / x) / np.spacing(1.0 / x)
+    ulp_q = np.abs(q - np.sqrt(x)) / np.spacing(np.sqrt(x))
+    assert ulp_r.max() <= 1.0, ulp_r.max()
+    assert ulp_q.max() <= 1.0, ulp_q.max()
+    z = np.zeros(1); r0 = np.empty(1); q0 = np.empty(1)
+    mmf.capi.check(lib.mmf_newton_selftest(1, mmf.capi.ptr(z), mmf.capi.ptr(r0), mmf.capi.ptr(q0)))
+    assert q0[0] == 0.0
+
+
+def test_fast_2d_with_nonzero_w(orc, mmf):
+    """A 2D state with non-zero z-momentum (a passive scalar in 2D) takes the
+    five-field kernels; the result still matches the oracle."""
+    case = mmf.problem.reference_case("vortex_xy", 2, 32, t_end=0.5)
+    m = oracle_mesh(orc, case)
+    U0 = m.initial_state()
+    U0[:, 3] = 0.05 * U0[:, 0] * np.sin(np.arange(m.ncells))
+    U0[:, 4] += 0.5 * U0[:, 3] ** 2 / U0[:, 0]
+    U_ref, t_ref, steps_ref = m.run(U0, case.cfl, t_end=0.5)
+    with case.solver(arith="fast") as s:
+        U, t, steps = s.run(U0, case.cfl, t_end=0.5)
+    assert steps == steps_ref
+    assert rel_err(U, U_ref) <= FAST_RTOL
+    assert np.abs(U[:, 3]).max() > 0.0
+
+
 # ---- computeRHS -------------------------------------------------------------------------
 
 RHS_CASES = [("vortex_xy", 2, 64), ("radsod", 2, 64), ("vortex_xy", 3, 16), ("vortex_yz", 3, 16),
