@@ -182,17 +182,22 @@ __device__ __forceinline__ void store_output(const StageArgs &sa, const GridPara
 }
 
 // Adds the two faces of direction d to the accumulator in reference order.
-template <class A>
+// The first pair of a cell starts the accumulator: the reference starts from
+// 0.0 (euler.cpp:142-148), which the reference arithmetic keeps so that signed
+// zeros match too; the fast arithmetic starts from the first difference.
+template <class A, bool FIRST>
 __device__ __forceinline__ void accumulate_pair(double *acc, const double *Flo, const double *Fhi, double area,
                                                 bool hi_first)
 {
 #pragma unroll
     for (int k = 0; k < A::NVAR; ++k) {
         if (IsExact<A>::value) {
+            if (FIRST) acc[k] = 0.0;
             if (hi_first) { acc[k] = acc[k] - area * Fhi[k]; acc[k] = acc[k] + area * Flo[k]; }
             else { acc[k] = acc[k] + area * Flo[k]; acc[k] = acc[k] - area * Fhi[k]; }
         } else {
-            acc[k] += Flo[k] - Fhi[k];
+            if (FIRST) acc[k] = Flo[k] - Fhi[k];
+            else acc[k] += Flo[k] - Fhi[k];
         }
     }
 }
@@ -308,18 +313,16 @@ __global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs s
         if (out_col) lmax = max_nonneg(lmax, l);
     }
     for (int y = y0; y < y1; ++y) {
+        // x faces of row y (the cell's x pair opens the accumulator)
+        const double lx = xfaces<A, 2>(cur, Fxlo, Fxhi);
+        if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
+        accumulate_pair<A, true>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
+        // row y+1 and the y face between y and y+1
         load_record<A, STAGE, 2>(sa, gp, sc, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
         const double ly = face_dir<A, 2>(cur, abv, 1, Fyhi);
-        const double lx = xfaces<A, 2>(cur, Fxlo, Fxhi);
-        if (STAGE <= STAGE_1) {
-            if (out_col) lmax = max_nonneg(lmax, ly);
-            if (xface_valid) lmax = max_nonneg(lmax, lx);
-        }
+        if (STAGE <= STAGE_1 && out_col) lmax = max_nonneg(lmax, ly);
         if (out_col) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-            accumulate_pair<A>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
-            accumulate_pair<A>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
+            accumulate_pair<A, false>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
             store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * y, acc, cur.c);
         }
         cur = abv;
@@ -340,20 +343,24 @@ __global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs s
 }
 
 // ---------------------------------------------------------------- 3D kernel
-// Block = BY warps stacked in y (rows y0-1 .. y0+BY-2; the first and last are
-// halo rows that only contribute y-face states), marching along z.
-template <int BY>
+// Block = BY warps stacked in y, rows y0-1 .. y0+BY-2, marching along z.
+// Warp 0 and warp BY-1 are halo rows: they only provide the y-face state of
+// their row (and warp BY-1 evaluates the y face below it); warps 1..BY-2
+// own the output rows.  Per plane: x faces (shuffles), y faces (shared
+// memory), then the next plane's record and the z face.
+template <int BY, int NV>
 struct Smem3D {
-    double c[BY][NF][32];
-    double f[BY][NF][32];
+    double c[BY][NV][32];
+    double f[BY][NV][32];
     double lam[BY][32];
-    double F[BY][NF][32];
+    double F[BY][NV][32];   // F[w] = face between rows w-1 and w
 };
 
 template <class A, int STAGE, int BY>
 __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageArgs sa)
 {
-    __shared__ Smem3D<BY> sm;
+    constexpr int NV = A::NVAR;
+    __shared__ Smem3D<BY, NV> sm;
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
@@ -369,8 +376,8 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
     const int y = rb * (BY - 2) - 1 + w;
     const int z0 = chunk * gp.chunk;
     const int z1 = min(z0 + gp.chunk, nz);
-    const bool halo_row = (w == 0) || (w == BY - 1);
-    const bool out_row = !halo_row && (y < ny);
+    const bool halo_lo = (w == 0), halo_hi = (w == BY - 1);
+    const bool out_row = !halo_lo && !halo_hi && (y < ny);
     const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
     const bool out = out_row && out_col;
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
@@ -380,57 +387,76 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
     double lmax = 0.0;
 
     RecOf<A, 3> cur, abv;
-    double Fzlo[NF], Fzhi[NF], Fxlo[NF], Fxhi[NF], Fylo[NF], Fyhi[NF], acc[NF];
-    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, abv, nullptr);
-    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
-    {
+    double Fzlo[NV], Fzhi[NV], Fa[NV], Fb[NV], acc[NV];
+    if (!halo_lo && !halo_hi) {
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, abv, nullptr);
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
         const double l = face_dir<A, 3>(abv, cur, 2, Fzlo);
-        if (out) lmax = fmax(lmax, l);
+        if (out) lmax = max_nonneg(lmax, l);
     }
     for (int z = z0; z < z1; ++z) {
-        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, abv, (z + 1 < z1) ? st : nullptr);
-        const double lz = face_dir<A, 3>(cur, abv, 2, Fzhi);
-        const double lx = xfaces<A, 3>(cur, Fxlo, Fxhi);
-        // y-faces through shared memory
+        if (halo_lo || halo_hi) {
+            // halo row: y-face state only (the compiler drops the unused fluxes)
+            RecOf<A, 3> h;
+            load_record<A, STAGE, 3>(sa, gp, sc, x, y, z, h, nullptr);
 #pragma unroll
-        for (int k = 0; k < NF; ++k) { sm.c[w][k][lane] = cur.c[k]; sm.f[w][k][lane] = cur.f[1][k]; }
+            for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = h.c[k]; sm.f[w][k][lane] = h.f[1][k]; }
+            sm.lam[w][lane] = h.lam[1];
+            __syncthreads();
+            if (halo_hi) {
+                double cL[NV], fL[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { cL[k] = sm.c[w - 1][k][lane]; fL[k] = sm.f[w - 1][k][lane]; }
+                const double ly = A::face(cL, fL, sm.lam[w - 1][lane], h.c, h.f[1], h.lam[1], Fa);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.F[w][k][lane] = Fa[k];
+                if (STAGE <= STAGE_1 && out_col && y - 1 < ny) lmax = max_nonneg(lmax, ly);
+            }
+            __syncthreads();
+            __syncthreads();
+            continue;
+        }
+        // x faces of plane z
+        const double lx = xfaces<A, 3>(cur, Fa, Fb);
+        if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = max_nonneg(lmax, lx);
+        accumulate_pair<A, true>(acc, Fa, Fb, gp.area, perx && x == nx - 1);
+        // y faces through shared memory: this warp evaluates the face below its row
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = cur.c[k]; sm.f[w][k][lane] = cur.f[1][k]; }
         sm.lam[w][lane] = cur.lam[1];
         __syncthreads();
-        double ly = 0.0;
-        if (w < BY - 1) {
-            double cR[NF], fR[NF];
+        {
+            double cL[NV], fL[NV];
 #pragma unroll
-            for (int k = 0; k < NF; ++k) { cR[k] = sm.c[w + 1][k][lane]; fR[k] = sm.f[w + 1][k][lane]; }
-            ly = A::face(cur.c, cur.f[1], cur.lam[1], cR, fR, sm.lam[w + 1][lane], Fyhi);
+            for (int k = 0; k < NV; ++k) { cL[k] = sm.c[w - 1][k][lane]; fL[k] = sm.f[w - 1][k][lane]; }
+            const double ly = A::face(cL, fL, sm.lam[w - 1][lane], cur.c, cur.f[1], cur.lam[1], Fa);
 #pragma unroll
-            for (int k = 0; k < NF; ++k) sm.F[w][k][lane] = Fyhi[k];
+            for (int k = 0; k < NV; ++k) sm.F[w][k][lane] = Fa[k];
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
         }
         __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fb[k] = sm.F[w + 1][k][lane];
+        accumulate_pair<A, false>(acc, Fa, Fb, gp.area, pery && y == ny - 1);
+        // plane z+1 and the z face
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, abv, (z + 1 < z1) ? st : nullptr);
+        const double lz = face_dir<A, 3>(cur, abv, 2, Fzhi);
+        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
         if (out) {
-#pragma unroll
-            for (int k = 0; k < NF; ++k) Fylo[k] = sm.F[w - 1][k][lane];
-            if (STAGE <= STAGE_1) {
-                lmax = fmax(lmax, fmax(lz, ly));
-                if (w == 1) lmax = fmax(lmax, sm.lam[0][lane] < cur.lam[1] ? cur.lam[1] : sm.lam[0][lane]);
-            }
-#pragma unroll
-            for (int k = 0; k < NF; ++k) acc[k] = 0.0;
-            accumulate_pair<A>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
-            accumulate_pair<A>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
-            accumulate_pair<A>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
+            accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
             store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
                                    acc, cur.c);
         }
-        if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = fmax(lmax, lx);
         __syncthreads();
         cur = abv;
 #pragma unroll
-        for (int k = 0; k < NF; ++k) Fzlo[k] = Fzhi[k];
+        for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
     }
     if (STAGE <= STAGE_1) {
         lmax = warp_max(lmax);
         if (lane == 0) {
-            unsigned long long* dst = (STAGE == STAGE_RHS) ? (unsigned long long*)sa.rhs_maxeig : &sa.ctrl->maxeig_bits;
+            unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
+                                                           : &sa.ctrl->maxeig_bits;
             atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
         }
         if (STAGE == STAGE_1) {

@@ -9,7 +9,7 @@
 
 namespace mmf {
 
-constexpr int BY3D = 8;         // warps per 3D block (6 output rows + 2 halo rows)
+constexpr int BY3D = 16;        // warps per 3D block (14 output rows + 2 halo rows)
 constexpr int WARPS_2D = 4;     // warps per 2D block
 
 // Fills the decomposition fields of gp for the given marching chunk.
@@ -21,7 +21,7 @@ inline void plan_cartesian(GridParams &gp, int chunk)
         gp.nchunk = (gp.n[1] + gp.chunk - 1) / gp.chunk;
         gp.nrowblk = 1;
     } else {
-        gp.chunk = chunk > 0 ? chunk : 16;
+        gp.chunk = chunk > 0 ? chunk : 32;
         gp.nchunk = (gp.n[2] + gp.chunk - 1) / gp.chunk;
         gp.nrowblk = (gp.n[1] + BY3D - 3) / (BY3D - 2);
     }
