@@ -1,0 +1,121 @@
+/*
+ * Drop-in check of the C++ adapter (include/minimmerflow_gb300.hpp): the
+ * reference time loop of src/main.cpp:377-506, written as in the reference,
+ * with euler::computeRHS and reconstruction::computePolynomials taken from
+ * mmf_gb300::.  Mesh and storage types are the bitpit stand-in of the oracle
+ * (test infrastructure); a small MeshGeometricalInfo-like class provides the
+ * accessors the adapter reads.  Initial states come from the C oracle.
+ *
+ * usage: test_dropin <radsod|vortex_xy> <dim> <nCells> <steps> <out_loop.bin> <out_stepper.bin>
+ */
+#include "bitpit_voloctree.hpp"
+#include "minimmerflow_gb300.hpp"
+#include "mmf_oracle.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace bitpit { namespace config { Config root; } }
+using namespace bitpit;
+
+typedef PiercedStorage<bool, long> CellStorageBool;
+typedef PiercedStorage<double, long> CellStorageDouble;
+typedef PiercedStorage<int, long> InterfaceStorageInt;
+
+class MeshInfoLike {
+public:
+    explicit MeshInfoLike(const VolumeKernel &patch) : m_patch(patch)
+    {
+        for (std::size_t r = 0; r < patch.getCells().size(); ++r) {
+            m_cells.push_back(r);
+            m_centroids.push_back(patch.evalCellCentroid((long)r));
+            m_sizes.push_back(patch.evalCellSize((long)r));
+            m_volumes.push_back(patch.evalCellVolume((long)r));
+        }
+        for (std::size_t r = 0; r < patch.getInterfaces().size(); ++r) {
+            m_interfaces.push_back(r);
+            m_normals.push_back(patch.evalInterfaceNormal((long)r));
+        }
+    }
+    int getDimension() const { return m_patch.getDimension(); }
+    const VolumeKernel &getPatch() const { return m_patch; }
+    const std::vector<std::size_t> &getCellRawIds() const { return m_cells; }
+    const std::vector<std::size_t> &getInterfaceRawIds() const { return m_interfaces; }
+    const std::array<double, 3> &rawGetCellCentroid(std::size_t r) const { return m_centroids[r]; }
+    double rawGetCellSize(std::size_t r) const { return m_sizes[r]; }
+    double rawGetCellVolume(std::size_t r) const { return m_volumes[r]; }
+    const std::array<double, 3> &rawGetInterfaceNormal(std::size_t r) const { return m_normals[r]; }
+
+private:
+    const VolumeKernel &m_patch;
+    std::vector<std::size_t> m_cells, m_interfaces;
+    std::vector<std::array<double, 3>> m_centroids, m_normals;
+    std::vector<double> m_sizes, m_volumes;
+};
+
+int main(int argc, char **argv)
+{
+    if (argc < 7) return 2;
+    const int problem = std::strcmp(argv[1], "radsod") == 0 ? ORC_RADSOD : ORC_VORTEX_XY;
+    const int dim = std::atoi(argv[2]);
+    const long n = std::atol(argv[3]);
+    const int steps = std::atoi(argv[4]);
+    std::array<double, 3> origin = (problem == ORC_RADSOD) ? std::array<double, 3>{{0., 0., 0.}}
+                                                           : std::array<double, 3>{{-5., -5., -5.}};
+    const double length = (problem == ORC_RADSOD) ? 8.0 : 10.0;
+    const double cfl = 0.45;
+    VolOctree mesh(dim, origin, length, length / n);
+    MeshInfoLike meshInfo(mesh);
+    const std::size_t nCells = meshInfo.getCellRawIds().size();
+
+    CellStorageBool solved(1, &mesh.getCells());
+    CellStorageDouble U(5, &mesh.getCells()), W(5, &mesh.getCells()), RHS(5, &mesh.getCells());
+    InterfaceStorageInt bcs(1, &mesh.getInterfaces());
+    for (std::size_t r = 0; r < nCells; ++r) solved.rawSet(r, true);
+    for (std::size_t f : meshInfo.getInterfaceRawIds())
+        bcs[(long)f] = mesh.getInterfaces().rawAt(f).isBorder()
+                           ? (problem == ORC_RADSOD ? MMF_BC_REFLECTING : MMF_BC_FREE_FLOW) : MMF_BC_NONE;
+    orc_params prm;
+    orc_params_default(&prm);
+    for (std::size_t r = 0; r < nCells; ++r)
+        orc_exact_conservatives(problem, dim, &prm, meshInfo.rawGetCellCentroid(r).data(), 0.0, U.rawData(r));
+    CellStorageDouble U0 = U;
+
+    const double minCellSize = meshInfo.rawGetCellSize(0);
+    double t = 0.0;
+    for (int step = 0; step < steps; ++step) {
+        double maxEig;
+        mmf_gb300::reconstruction::computePolynomials(problem, meshInfo, solved, U, bcs);
+        mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, U, bcs, &RHS, &maxEig);
+        double dt = 0.9 * cfl * minCellSize / maxEig;
+        for (std::size_t r = 0; r < nCells; ++r)
+            for (int k = 0; k < 5; ++k) W.rawData(r)[k] = U.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r);
+        mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, W, bcs, &RHS, &maxEig);
+        for (std::size_t r = 0; r < nCells; ++r)
+            for (int k = 0; k < 5; ++k)
+                W.rawData(r)[k] = 0.75 * U.rawData(r)[k] + 0.25 * (W.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r));
+        mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, W, bcs, &RHS, &maxEig);
+        for (std::size_t r = 0; r < nCells; ++r)
+            for (int k = 0; k < 5; ++k)
+                U.rawData(r)[k] = (1. / 3) * U.rawData(r)[k] + (2. / 3) * (W.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r));
+        t += dt;
+    }
+    FILE *fp = std::fopen(argv[5], "wb");
+    std::fwrite(U.rawData(0), sizeof(double), 5 * nCells, fp);
+    std::fclose(fp);
+
+    // the same run kept on the device
+    mmf_gb300::Stepper stepper(meshInfo, bcs, MMF_ARITH_REFERENCE);
+    stepper.upload(U0);
+    stepper.setTime(cfl, 0.0, INFINITY, steps);
+    double t2 = 0.0;
+    const int64_t done = stepper.run(&t2);
+    stepper.download(&U0);
+    fp = std::fopen(argv[6], "wb");
+    std::fwrite(U0.rawData(0), sizeof(double), 5 * nCells, fp);
+    std::fclose(fp);
+    std::printf("steps %d %lld t %.17g %.17g\n", steps, (long long)done, t, t2);
+    mmf_gb300::releaseContext(meshInfo);
+    return (done == steps && t == t2) ? 0 : 1;
+}
