@@ -140,6 +140,27 @@ int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, co
 int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
                        const double *dirichlet_prim, double *cons_bc);
 
+/* ---- residual without device allocation ------------------------------- */
+/* Largest mesh accepted by mmf_compute_rhs_noalloc. */
+#define MMF_NOALLOC_MAX_CELLS 65536
+/* euler::computeRHS for callers that cannot call cudaMalloc (for example code
+ * running while another library captures a CUDA graph, real-time loops that
+ * cannot take the synchronisation an allocation implies, or processes whose
+ * device memory is held by a pool allocator).  No counterpart in the
+ * reference.  Inputs and outputs are device pointers: d_cons and d_rhs are
+ * AoS double[n][5] in raw order, d_max_eig one double, d_raw_to_cell an
+ * optional raw -> grid-cell permutation (NULL = row-major).  Work is queued
+ * on 'stream' (a cudaStream_t, NULL = the default stream) on the current
+ * device and the call returns without waiting.  The working set lives in a
+ * static device array of 2*5*MMF_NOALLOC_MAX_CELLS + 32 doubles (about 5.2 MB)
+ * that every GPU which loads the library holds until exit; meshes with more
+ * cells are rejected with MMF_ERR_ARG.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  Reference arithmetic: the result equals mmf_compute_rhs bit for bit. */
+int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_cons, double *d_rhs, double *d_max_eig,
+                            const int64_t *d_raw_to_cell, void *stream);
+
 /* Self-test of the reciprocal and square root of MMF_ARITH_FAST (Newton
  * iterations on the hardware approximations): rcp[i] ~ 1/x[i], sqrt[i] ~ sqrt(x[i])
  * for positive x.  No reference counterpart; used to check the error bound. */

@@ -20,8 +20,9 @@ EXPORTS = [
     "mmf_download_state_device", "mmf_compute_rhs", "mmf_compute_polynomials", "mmf_time_setup",
     "mmf_advance", "mmf_advance_async", "mmf_time_info", "mmf_get_stream", "mmf_advance_host", "mmf_last_step_info", "mmf_get_status", "mmf_synchronize",
     "mmf_rk_stage", "mmf_cons2prim", "mmf_prim2cons", "mmf_eval_fluxes", "mmf_eval_splitting",
-    "mmf_eval_bc_values", "mmf_newton_selftest",
+    "mmf_eval_bc_values", "mmf_newton_selftest", "mmf_compute_rhs_noalloc",
 ]
+NOALLOC_MAX_CELLS = 65536
 
 
 class Grid(C.Structure):
@@ -78,6 +79,7 @@ def load(build_if_missing=True):
     L.mmf_eval_splitting.argtypes = [C.c_int64, _P, _P, _P, _P, _P]
     L.mmf_eval_bc_values.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P]
     L.mmf_newton_selftest.argtypes = [C.c_int64, _P, _P, _P]
+    L.mmf_compute_rhs_noalloc.argtypes = [C.POINTER(Grid), _P, _P, _P, _P, _P]
     _lib = L
     return L
 

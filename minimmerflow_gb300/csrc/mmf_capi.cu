@@ -67,6 +67,11 @@ __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__rest
 
 } // namespace
 
+namespace mmf {
+// Records an error for mmf_last_error() from another translation unit.
+int set_last_error(int code, const char *msg) { return fail(code, msg); }
+}
+
 struct mmf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
