@@ -164,7 +164,8 @@ template <class ProblemType, class MeshInfo, class CellStorageBool, class CellSt
 void computePolynomials(ProblemType, const MeshInfo &meshInfo, const CellStorageBool &, const CellStorageDouble &,
                         const InterfaceStorageInt &interfaceBCs)
 {
-    check(mmf_compute_polynomials(contextFor(meshInfo, interfaceBCs, 1).get()));
+    Context &ctx = contextFor(meshInfo, interfaceBCs, 1);
+    check(mmf_compute_polynomials(ctx.get(), nullptr, nullptr, nullptr, ctx.nCells()));
 }
 }
 

@@ -67,7 +67,8 @@ typedef struct {
     double h;                  /* cell edge = minCellSize (src/main.cpp:351-356) */
     int bc_lo[3], bc_hi[3];    /* border condition per side (MMF_BC_*) */
     double dirichlet_prim[5];  /* (p,u,v,w,T) behind MMF_BC_DIRICHLET borders (src/problem.cpp:458-468) */
-    int order;                 /* reconstruction order: 1 (src/reconstruction.cpp:67-79) */
+    int order;                 /* reconstruction order: 1 (src/reconstruction.cpp:67-79), or 2 (MC-limited
+                                  MUSCL on the computePolynomials hook; no reference implementation) */
     int arith;                 /* MMF_ARITH_* */
     int chunk;                 /* marching chunk (rows 2D / planes 3D); 0 = default */
 } mmf_grid;
@@ -97,9 +98,25 @@ int mmf_download_state_device(mmf_ctx *ctx, double *d_aos, int64_t n_raw);
  * divided by the volume) and the maximum face eigenvalue, for the state
  * 'cons' (host AoS raw layout).  Always uses the reference arithmetic. */
 int mmf_compute_rhs(mmf_ctx *ctx, const double *cons, double *rhs, double *max_eig, int64_t n_raw);
-/* reconstruction::computePolynomials (src/reconstruction.hpp:41-42) on the
- * uploaded state: a no-op at order 1. */
-int mmf_compute_polynomials(mmf_ctx *ctx);
+/* reconstruction::computePolynomials (src/reconstruction.hpp:41-42) of the
+ * state 'cons' (host AoS raw layout): a no-op at order 1.  At order 2 it
+ * computes the limited slopes (returned as AoS [n_raw][3][5] when 'slopes' is
+ * not NULL, direction-major) and the cells where the limiter changed a slope
+ * ('limiter_active', one byte per raw id, when not NULL). */
+int mmf_compute_polynomials(mmf_ctx *ctx, const double *cons, double *slopes, unsigned char *limiter_active,
+                            int64_t n_raw);
+/* Order-2 limiter selection: MMF_LIMIT_ALL (every cell), MMF_LIMIT_NONE
+ * (central slopes), MMF_LIMIT_FLAGGED (cells whose byte in 'flags', raw order,
+ * is non-zero; flags may be NULL to keep the uploaded ones). */
+#define MMF_LIMIT_ALL 0
+#define MMF_LIMIT_NONE 1
+#define MMF_LIMIT_FLAGGED 2
+int mmf_set_limiter(mmf_ctx *ctx, int mode, const unsigned char *flags, int64_t n_raw);
+/* Flags already on the device, one byte per grid cell (grid order); selects MMF_LIMIT_FLAGGED. */
+int mmf_set_limiter_flags_device(mmf_ctx *ctx, const unsigned char *d_flags_grid);
+/* Where the limiter changed a slope at stage 1 of the last step (or the last
+ * mmf_compute_polynomials call): one byte per raw id. */
+int mmf_get_limiter_activity(mmf_ctx *ctx, unsigned char *active, int64_t n_raw);
 
 /* ---- time loop (src/main.cpp:377-506) on the uploaded state ----------- */
 /* Sets t, t_end (INFINITY allowed with max_steps >= 0), CFL; minCellSize = h. */

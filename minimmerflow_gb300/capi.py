@@ -20,8 +20,10 @@ EXPORTS = [
     "mmf_download_state_device", "mmf_compute_rhs", "mmf_compute_polynomials", "mmf_time_setup",
     "mmf_advance", "mmf_advance_async", "mmf_time_info", "mmf_get_stream", "mmf_advance_host", "mmf_last_step_info", "mmf_get_status", "mmf_synchronize",
     "mmf_rk_stage", "mmf_cons2prim", "mmf_prim2cons", "mmf_eval_fluxes", "mmf_eval_splitting",
-    "mmf_eval_bc_values", "mmf_newton_selftest", "mmf_compute_rhs_noalloc",
+    "mmf_eval_bc_values", "mmf_newton_selftest", "mmf_compute_rhs_noalloc", "mmf_set_limiter",
+    "mmf_set_limiter_flags_device", "mmf_get_limiter_activity",
 ]
+LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
 
 
@@ -61,7 +63,10 @@ def load(build_if_missing=True):
     for name in ("mmf_upload_state", "mmf_download_state", "mmf_upload_state_device", "mmf_download_state_device"):
         getattr(L, name).argtypes = [_P, _P, C.c_int64]
     L.mmf_compute_rhs.argtypes = [_P, _P, _P, _D, C.c_int64]
-    L.mmf_compute_polynomials.argtypes = [_P]
+    L.mmf_compute_polynomials.argtypes = [_P, _P, _P, _P, C.c_int64]
+    L.mmf_set_limiter.argtypes = [_P, C.c_int, _P, C.c_int64]
+    L.mmf_set_limiter_flags_device.argtypes = [_P, _P]
+    L.mmf_get_limiter_activity.argtypes = [_P, _P, C.c_int64]
     L.mmf_time_setup.argtypes = [_P, C.c_double, C.c_double, C.c_double, C.c_int64]
     L.mmf_advance.argtypes = [_P, C.c_int64, _D, C.POINTER(C.c_int64)]
     L.mmf_advance_async.argtypes = [_P, C.c_int64]

@@ -89,6 +89,11 @@ struct mmf_ctx {
     bool time_ready = false;
     bool w_zero = false;      // 2D state with identically zero z-momentum
     int *flag = nullptr;      // device scratch flag
+    // order 2
+    double *Sl = nullptr;               // slopes, dim x 5 planes
+    unsigned char *lim_flag = nullptr;  // per cell: limit (1) / central slope (0) in LIMIT_FLAGGED mode
+    unsigned char *lim_active = nullptr;// per cell: the limiter changed a slope (stage 1 of the last step)
+    int limit_mode = LIMIT_ALL;
 
     cudaError_t stage(int st, const double *U_in, double *out)
     {
@@ -103,13 +108,36 @@ struct mmf_ctx {
         return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_stage_fast(st, gp, sa, stream, w_zero)
                                                                 : launch_stage_exact(st, gp, sa, stream);
     }
+    cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
+    {
+        StageArgs sa;
+        sa.U = U; sa.R = R; sa.W = W; sa.out = out; sa.ctrl = ctrl; sa.rhs_maxeig = rhs_maxeig;
+        O2Args oa;
+        oa.state = state; oa.S = Sl; oa.flag = lim_flag; oa.active = active; oa.limit_mode = limit_mode;
+        oa.ctrl = ctrl; oa.stage = st;
+        ++launches;
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_o2_fast(op, st, gp, sa, oa, W, stream, w_zero)
+                                                                : launch_o2_exact(op, st, gp, sa, oa, W, stream);
+    }
     cudaError_t rk_step()
     {
         cudaError_t e;
+        if (grid.order == 2) {
+            // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
+            // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
+            if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
+            if ((e = o2(O2_STAGE, STAGE_1, U, R, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_FORM_W1, STAGE_2, U, W, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_SLOPES, STAGE_2, W, nullptr, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_STAGE, STAGE_2, W, R, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_SLOPES, STAGE_3, R, nullptr, nullptr)) != cudaSuccess) return e;
+            return o2(O2_STAGE, STAGE_3, R, U, nullptr);
+        }
         if ((e = stage(STAGE_1, U, R)) != cudaSuccess) return e;
         if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U, U);
     }
+    int launches_per_step() const { return grid.order == 2 ? 7 : 3; }
 };
 
 static int check_ctx(mmf_ctx *ctx)
@@ -143,8 +171,8 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
         }
     }
     if (!(grid->h > 0.0)) return fail(MMF_ERR_ARG, "h must be > 0");
-    if (grid->order != 1)   // src/reconstruction.cpp:75-76 exits on any other order
-        return fail(MMF_ERR_UNSUPPORTED, "only order 1 is supported by this context type");
+    if (grid->order != 1 && grid->order != 2)   // src/reconstruction.cpp:75-76 exits on any other order
+        return fail(MMF_ERR_UNSUPPORTED, "reconstruction order must be 1 or 2");
     if (grid->arith != MMF_ARITH_REFERENCE && grid->arith != MMF_ARITH_FAST)
         return fail(MMF_ERR_ARG, "unknown arithmetic");
     int ndev = 0;
@@ -169,7 +197,7 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     const double h = grid->h;
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;
-    plan_cartesian(gp, grid->chunk);
+    plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D);
     const size_t bytes = sizeof(double) * NF * (size_t)gp.plane;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->U, bytes);
@@ -179,6 +207,13 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     if (e == cudaSuccess) e = cudaMalloc(&c->ctrl, sizeof(Ctrl));
     if (e == cudaSuccess) e = cudaMalloc(&c->rhs_maxeig, sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&c->flag, sizeof(int));
+    if (e == cudaSuccess && grid->order == 2) {
+        e = cudaMalloc(&c->Sl, bytes * grid->dim);
+        if (e == cudaSuccess) e = cudaMalloc(&c->lim_flag, (size_t)gp.plane);
+        if (e == cudaSuccess) e = cudaMalloc(&c->lim_active, (size_t)gp.plane);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->lim_flag, 0, (size_t)gp.plane, c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->lim_active, 0, (size_t)gp.plane, c->stream);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(c->U, 0, bytes, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->ctrl, 0, sizeof(Ctrl), c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -200,6 +235,7 @@ int mmf_destroy(mmf_ctx *c)
     if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
     cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
+    cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MMF_OK;
@@ -321,7 +357,10 @@ int mmf_compute_rhs(mmf_ctx *c, const double *cons, double *rhs, double *max_eig
     if ((rc = to_soa(c, c->aos, c->S, n_raw))) return rc;
     MMF_CUDA(cudaMemsetAsync(c->rhs_maxeig, 0, sizeof(double), c->stream));
     // the residual of stage 'RHS' lands in R; S is the input state
-    {
+    if (c->grid.order == 2) {
+        MMF_CUDA(c->o2(O2_SLOPES, STAGE_RHS, c->S, nullptr, nullptr));
+        MMF_CUDA(c->o2(O2_STAGE, STAGE_RHS, c->S, c->R, nullptr));
+    } else {
         StageArgs sa;
         sa.U = c->S; sa.R = c->R; sa.W = c->W; sa.out = c->R; sa.ctrl = c->ctrl; sa.rhs_maxeig = c->rhs_maxeig;
         ++c->launches;
@@ -336,11 +375,116 @@ int mmf_compute_rhs(mmf_ctx *c, const double *cons, double *rhs, double *max_eig
     return MMF_OK;
 }
 
-int mmf_compute_polynomials(mmf_ctx *c)
+// grid-order byte array <-> raw order
+__global__ void bytes_to_raw_kernel(const unsigned char *grid_v, unsigned char *raw_v, long long n,
+                                    const long long *raw_to_cell)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const long long g = raw_to_cell ? raw_to_cell[r] : r;
+    raw_v[r] = (g >= 0 && g < n) ? grid_v[g] : 0;
+}
+
+__global__ void bytes_from_raw_kernel(const unsigned char *raw_v, unsigned char *grid_v, long long n,
+                                      const long long *raw_to_cell)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const long long g = raw_to_cell ? raw_to_cell[r] : r;
+    if (g >= 0 && g < n) grid_v[g] = raw_v[r];
+}
+
+// slopes planes (grid order) -> AoS [n_raw][3][5] (raw order)
+__global__ void slopes_to_raw_kernel(const double *S, double *out, long long n, int dim, const long long *raw_to_cell)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const long long g = raw_to_cell ? raw_to_cell[r] : r;
+    if (g < 0 || g >= n) return;
+    for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < NF; ++k) out[(r * 3 + d) * NF + k] = (d < dim) ? S[(long long)(d * NF + k) * n + g] : 0.0;
+}
+
+int mmf_compute_polynomials(mmf_ctx *c, const double *cons, double *slopes, unsigned char *limiter_active,
+                            int64_t n_raw)
 {
     int rc = check_ctx(c);
     if (rc) return rc;
-    return MMF_OK;   // order 1: src/reconstruction.cpp:47-55 is empty
+    if (c->grid.order == 1) return MMF_OK;   // src/reconstruction.cpp:47-55 is empty at order 1
+    if (!cons || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    const size_t bytes = sizeof(double) * NF * (size_t)n_raw;
+    if (!c->S) MMF_CUDA(cudaMalloc(&c->S, bytes));
+    MMF_CUDA(cudaMemcpyAsync(c->aos, cons, bytes, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = to_soa(c, c->aos, c->S, n_raw))) return rc;
+    MMF_CUDA(c->o2(O2_SLOPES, STAGE_RHS, c->S, nullptr, c->lim_active));
+    const unsigned blocks = (unsigned)((n_raw + 255) / 256);
+    if (slopes) {
+        double *tmp = nullptr;
+        MMF_CUDA(cudaMalloc(&tmp, bytes * 3));
+        slopes_to_raw_kernel<<<blocks, 256, 0, c->stream>>>(c->Sl, tmp, n_raw, c->grid.dim, c->raw_to_cell);
+        ++c->launches;
+        cudaError_t e = cudaMemcpyAsync(slopes, tmp, bytes * 3, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(tmp);
+        MMF_CUDA(e);
+    }
+    if (limiter_active) return mmf_get_limiter_activity(c, limiter_active, n_raw);
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_set_limiter(mmf_ctx *c, int mode, const unsigned char *flags, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (mode != LIMIT_ALL && mode != LIMIT_NONE && mode != LIMIT_FLAGGED) return fail(MMF_ERR_ARG, "unknown limiter mode");
+    if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the limiter applies to order 2");
+    if (flags) {
+        if (n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "flag count must equal the cell count");
+        unsigned char *tmp = nullptr;
+        MMF_CUDA(cudaMalloc(&tmp, (size_t)n_raw));
+        cudaError_t e = cudaMemcpyAsync(tmp, flags, (size_t)n_raw, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) {
+            bytes_from_raw_kernel<<<(unsigned)((n_raw + 255) / 256), 256, 0, c->stream>>>(tmp, c->lim_flag, n_raw,
+                                                                                          c->raw_to_cell);
+            ++c->launches;
+            e = cudaPeekAtLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(tmp);
+        MMF_CUDA(e);
+    }
+    c->limit_mode = mode;
+    return MMF_OK;
+}
+
+int mmf_set_limiter_flags_device(mmf_ctx *c, const unsigned char *d_flags_grid)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->grid.order != 2 || !d_flags_grid) return fail(MMF_ERR_ARG, "order-2 context and flags required");
+    MMF_CUDA(cudaMemcpyAsync(c->lim_flag, d_flags_grid, (size_t)c->gp.plane, cudaMemcpyDeviceToDevice, c->stream));
+    c->limit_mode = LIMIT_FLAGGED;
+    return MMF_OK;
+}
+
+int mmf_get_limiter_activity(mmf_ctx *c, unsigned char *active, int64_t n_raw)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the limiter applies to order 2");
+    if (!active || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad buffer");
+    unsigned char *tmp = nullptr;
+    MMF_CUDA(cudaMalloc(&tmp, (size_t)n_raw));
+    bytes_to_raw_kernel<<<(unsigned)((n_raw + 255) / 256), 256, 0, c->stream>>>(c->lim_active, tmp, n_raw,
+                                                                                c->raw_to_cell);
+    ++c->launches;
+    cudaError_t e = cudaPeekAtLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(active, tmp, (size_t)n_raw, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    MMF_CUDA(e);
+    return MMF_OK;
 }
 
 int mmf_time_setup(mmf_ctx *c, double cfl, double t, double t_end, int64_t max_steps)
@@ -392,12 +536,12 @@ int mmf_advance(mmf_ctx *c, int64_t n_steps, double *t_out, int64_t *steps_done)
     int64_t left = n_steps;
     while (left >= GRAPH_STEPS) {
         MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
-        c->launches += 3 * GRAPH_STEPS;
+        c->launches += c->launches_per_step() * GRAPH_STEPS;
         left -= GRAPH_STEPS;
     }
     while (left-- > 0) {
         MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
-        c->launches += 3;
+        c->launches += c->launches_per_step();
     }
     Ctrl after;
     MMF_CUDA(cudaMemcpyAsync(&after, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
@@ -419,12 +563,12 @@ int mmf_advance_async(mmf_ctx *c, int64_t n_steps)
     int64_t left = n_steps;
     while (left >= GRAPH_STEPS) {
         MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
-        c->launches += 3 * GRAPH_STEPS;
+        c->launches += c->launches_per_step() * GRAPH_STEPS;
         left -= GRAPH_STEPS;
     }
     while (left-- > 0) {
         MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
-        c->launches += 3;
+        c->launches += c->launches_per_step();
     }
     return MMF_OK;
 }
@@ -459,6 +603,27 @@ int mmf_rk_stage(mmf_ctx *c, int stage)
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    if (c->grid.order == 2) {
+        cudaError_t e2 = cudaSuccess;
+        switch (stage) {
+        case 1:
+            e2 = c->o2(O2_SLOPES, STAGE_1, c->U, nullptr, c->lim_active);
+            if (e2 == cudaSuccess) e2 = c->o2(O2_STAGE, STAGE_1, c->U, c->R, nullptr);
+            break;
+        case 2:
+            e2 = c->o2(O2_FORM_W1, STAGE_2, c->U, c->W, nullptr);
+            if (e2 == cudaSuccess) e2 = c->o2(O2_SLOPES, STAGE_2, c->W, nullptr, nullptr);
+            if (e2 == cudaSuccess) e2 = c->o2(O2_STAGE, STAGE_2, c->W, c->R, nullptr);
+            break;
+        case 3:
+            e2 = c->o2(O2_SLOPES, STAGE_3, c->R, nullptr, nullptr);
+            if (e2 == cudaSuccess) e2 = c->o2(O2_STAGE, STAGE_3, c->R, c->U, nullptr);
+            break;
+        default: return fail(MMF_ERR_ARG, "stage must be 1, 2 or 3");
+        }
+        if (e2 != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e2));
+        return MMF_OK;
+    }
     cudaError_t e;
     switch (stage) {
     case 1: e = c->stage(STAGE_1, c->U, c->R); break;

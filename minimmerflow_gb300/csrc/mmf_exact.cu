@@ -11,6 +11,12 @@ cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs 
     return launch_stage<ExactArith>(stage, gp, sa, s);
 }
 
+cudaError_t launch_o2_exact(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
+                            double *W1, cudaStream_t s)
+{
+    return launch_o2<ExactArith>(op, stage, gp, sa, oa, W1, s);
+}
+
 // One thread per item; arrays are AoS [n][5] (normals [n][3]).
 __global__ void pointwise_kernel(int op, long long n, const double *a, const double *b, const double *nrm, int bc,
                                  const double *dir_prim, double *out, double *out2)

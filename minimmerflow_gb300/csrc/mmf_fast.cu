@@ -10,6 +10,13 @@ cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &
     return launch_stage<FastArith>(stage, gp, sa, s);
 }
 
+cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
+                           double *W1, cudaStream_t s, bool w_zero)
+{
+    if (gp.dim == 2 && w_zero) return launch_o2<FastArith2DW0, false>(op, stage, gp, sa, oa, W1, s);
+    return launch_o2<FastArith>(op, stage, gp, sa, oa, W1, s);
+}
+
 __global__ void newton_selftest_kernel(long long n, const double *x, double *r, double *q)
 {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;

@@ -6,14 +6,17 @@
 #include <cuda_runtime.h>
 
 #include "mmf_cartesian.cuh"
+#include "mmf_order2.cuh"
 
 namespace mmf {
 
 constexpr int BY3D = 16;        // warps per 3D block (14 output rows + 2 halo rows)
 constexpr int WARPS_2D = 4;     // warps per 2D block
+constexpr int BY3D_O2 = 8;      // warps per 3D order-2 block (face-side records need twice the registers)
 
-// Fills the decomposition fields of gp for the given marching chunk.
-inline void plan_cartesian(GridParams &gp, int chunk)
+// Fills the decomposition fields of gp for the given marching chunk; 'by' is
+// the number of warps a 3D block stacks in y (two of them halo rows).
+inline void plan_cartesian(GridParams &gp, int chunk, int by = 16)
 {
     gp.nseg = (gp.n[0] + SEG - 1) / SEG;
     if (gp.dim == 2) {
@@ -23,7 +26,7 @@ inline void plan_cartesian(GridParams &gp, int chunk)
     } else {
         gp.chunk = chunk > 0 ? chunk : 32;
         gp.nchunk = (gp.n[2] + gp.chunk - 1) / gp.chunk;
-        gp.nrowblk = (gp.n[1] + BY3D - 3) / (BY3D - 2);
+        gp.nrowblk = (gp.n[1] + by - 3) / (by - 2);
     }
     gp.plane = (long long)gp.n[0] * gp.n[1] * gp.n[2];
 }
@@ -62,6 +65,60 @@ inline cudaError_t launch_stage(int stage, const GridParams &gp, const StageArgs
     default: return cudaErrorInvalidValue;
     }
 }
+
+// ---- order 2 --------------------------------------------------------------
+enum O2Op { O2_SLOPES = 0, O2_FORM_W1 = 1, O2_STAGE = 2 };
+
+inline unsigned elementwise_blocks(long long n)
+{
+    long long b = (n + 255) / 256;
+    return (unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
+}
+
+template <class A, int STAGE, bool HAS3D>
+inline cudaError_t launch_o2_stage_t(const GridParams &gp, const StageArgs &sa, const O2Args &oa, cudaStream_t s)
+{
+    const unsigned blocks = (unsigned)cartesian_blocks(gp);
+    if (gp.dim == 2) {
+        stage2d_o2_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa, oa.state, oa.S);
+    } else {
+        if constexpr (HAS3D) stage3d_o2_kernel<A, STAGE, BY3D_O2><<<blocks, BY3D_O2 * 32, 0, s>>>(gp, sa, oa.state, oa.S);
+        else return cudaErrorInvalidValue;
+    }
+    return cudaPeekAtLastError();
+}
+
+template <class A, bool HAS3D = true>
+inline cudaError_t launch_o2(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
+                             double *W1, cudaStream_t s)
+{
+    switch (op) {
+    case O2_SLOPES:
+        if (gp.dim == 2) slopes_kernel<A, 2><<<elementwise_blocks(gp.plane), 256, 0, s>>>(gp, oa);
+        else {
+            if constexpr (HAS3D) slopes_kernel<A, 3><<<elementwise_blocks(gp.plane), 256, 0, s>>>(gp, oa);
+            else return cudaErrorInvalidValue;
+        }
+        return cudaPeekAtLastError();
+    case O2_FORM_W1:
+        form_w1_kernel<A><<<elementwise_blocks((long long)A::NVAR * gp.plane), 256, 0, s>>>(gp, sa, W1);
+        return cudaPeekAtLastError();
+    case O2_STAGE:
+        switch (stage) {
+        case STAGE_RHS: return launch_o2_stage_t<A, STAGE_RHS, HAS3D>(gp, sa, oa, s);
+        case STAGE_1: return launch_o2_stage_t<A, STAGE_1, HAS3D>(gp, sa, oa, s);
+        case STAGE_2: return launch_o2_stage_t<A, STAGE_2, HAS3D>(gp, sa, oa, s);
+        case STAGE_3: return launch_o2_stage_t<A, STAGE_3, HAS3D>(gp, sa, oa, s);
+        default: return cudaErrorInvalidValue;
+        }
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_o2_exact(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
+                            double *W1, cudaStream_t s);
+cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
+                           double *W1, cudaStream_t s, bool w_zero);
 
 // Entry points of the two arithmetic translation units.  w_zero selects the
 // 2D kernels that skip the identically-zero z-momentum.

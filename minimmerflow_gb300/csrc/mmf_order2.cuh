@@ -1,0 +1,482 @@
+// mmf_order2.cuh -- order-2 limited reconstruction on the uniform Cartesian grid.
+//
+// The reference's reconstruction has a polynomial hook, reconstruction::
+// computePolynomials (reconstruction.cpp:47-55), and evaluates order 1 only
+// (reconstruction.cpp:67-79); order 2 is a project extension on that hook:
+//
+//   slopes_kernel       computePolynomials: MUSCL slopes per direction and
+//                       conservative field with the monotonised-central (MC)
+//                       limiter sigma = minmod(2a, 2b, (a+b)/2), a = U_i - U_{i-1},
+//                       b = U_{i+1} - U_i (border neighbours are the ghost states
+//                       of euler.cpp:261-376), then a positivity fallback: if any
+//                       face state U +- sigma/2 has rho <= 0 or p <= 0 the cell
+//                       falls back to order 1.  A per-cell flag (limit / central)
+//                       selects the limiter; the kernel reports where the limiter
+//                       changed a slope (the troubled-cell labels).
+//   stage2d_o2_kernel / stage3d_o2_kernel
+//                       computeRHS with face states U +- sigma/2: every cell
+//                       evaluates a record per face side; border faces use the
+//                       ghost of the reconstructed face state, as the reference's
+//                       face loop does (euler.cpp:197-226).
+//   form_w1_kernel      W1 = U + dt R1 / V materialised for stage 2 (the
+//                       slopes need W1 at the neighbours).
+//
+// Buffers per step: U, R (stage-1 residual, then the stage-2 result W2 in
+// place), W (W1), S (slopes, DIM x NV planes), flags.
+#pragma once
+
+#include "mmf_cartesian.cuh"
+
+namespace mmf {
+
+// Limiter modes (per launch): every cell, no cell (central slopes), or the
+// cells whose flag byte is non-zero.
+enum { LIMIT_ALL = 0, LIMIT_NONE = 1, LIMIT_FLAGGED = 2 };
+
+struct O2Args {
+    const double *state;     // stage state planes (U, W1 or W2)
+    double *S;               // slopes: plane (d * NV + k)
+    const unsigned char *flag;
+    unsigned char *active;   // nullable: 1 where the limiter changed a slope
+    int limit_mode;
+    Ctrl *ctrl;
+    int stage;               // 0 = residual-only call, 1..3 = RK stage
+};
+
+// a*b <= 0 -> 0; else sign(a) min(2|a|, 2|b|, |a+b|/2)  (oracle orc_compute_polynomials)
+template <class A>
+__device__ __forceinline__ double mc_slope(double a, double b, double central)
+{
+    if (IsExact<A>::value) {
+        if (a * b <= 0.0) return 0.0;
+        double lim = fmin(2.0 * fabs(a), 2.0 * fabs(b));
+        double mag = fmin(lim, fabs(central));
+        return (a > 0.0) ? mag : -mag;
+    } else {
+        if (a * b <= 0.0) return 0.0;
+        const double mag = fmin(fmin(2.0 * fabs(a), 2.0 * fabs(b)), fabs(central));
+        return (a > 0.0) ? mag : -mag;
+    }
+}
+
+// division-free admissibility of a state: rho > 0 and 2 rho E > |m|^2
+template <class A>
+__device__ __forceinline__ bool admissible(const double *c)
+{
+    constexpr int NV = A::NVAR;
+    if (!(c[0] > 0.0)) return false;
+    double m2 = c[1] * c[1] + c[2] * c[2];
+    if (NV == 5) m2 = m2 + c[3] * c[3];
+    return (2.0 * c[0] * c[NV - 1] - m2) > 0.0;
+}
+
+template <class A>
+__device__ __forceinline__ void load_plain(const double *planes, long long plane, long long g, double *c)
+{
+#pragma unroll
+    for (int k = 0; k < A::NVAR; ++k) c[k] = __ldg(planes + (long long)A::field(k) * plane + g);
+}
+
+// computePolynomials: one thread per cell (grid-stride).
+template <class A, int DIM>
+__global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
+{
+    constexpr int NV = A::NVAR;
+    if (oa.stage >= 1) {
+        const Ctrl *ctrl = oa.ctrl;
+        const bool active = (oa.stage == 1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps)
+                                            : ctrl->active != 0;
+        if (!active) return;
+    }
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    const long long n = gp.plane;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int ix = (int)(g % nx);
+        const int iy = (int)((g / nx) % ny);
+        const int iz = (DIM == 3) ? (int)(g / ((long long)nx * ny)) : 0;
+        const int idx[3] = {ix, iy, iz};
+        double uc[NV];
+        load_plain<A>(oa.state, n, g, uc);
+        const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
+        bool act = false;
+        double sig[DIM][NV];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            double ul[NV], ur[NV];
+            for (int s = 0; s < 2; ++s) {
+                double *u = s ? ur : ul;
+                const int q = idx[d] + (s ? 1 : -1);
+                const bool per = gp.bc_lo[d] == BC_PERIODIC;
+                if (q >= 0 && q < gp.n[d]) {
+                    const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
+                    load_plain<A>(oa.state, n, g + (s ? stride : -stride), u);
+                } else if (per) {
+                    const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
+                    const long long wrap = (long long)(gp.n[d] - 1) * stride;
+                    load_plain<A>(oa.state, n, s ? g - wrap : g + wrap, u);
+                } else {
+                    double nrm[3] = {0.0, 0.0, 0.0};
+                    nrm[d] = s ? 1.0 : -1.0;
+                    ghost_state<A>(s ? gp.bc_hi[d] : gp.bc_lo[d], nrm, uc, gp.dir_prim, u);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double a = uc[k] - ul[k];
+                const double b = ur[k] - uc[k];
+                const double central = 0.5 * (a + b);
+                double sl = central;
+                if (limit) {
+                    sl = mc_slope<A>(a, b, central);
+                    if (sl != central) act = true;
+                }
+                sig[d][k] = sl;
+            }
+        }
+        if (limit) {
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                double fm[NV], fp[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { fm[k] = uc[k] - 0.5 * sig[d][k]; fp[k] = uc[k] + 0.5 * sig[d][k]; }
+                ok = ok && admissible<A>(fm) && admissible<A>(fp);
+            }
+            if (!ok) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) sig[d][k] = 0.0;
+                act = true;
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = sig[d][k];
+        if (oa.active) oa.active[g] = act ? 1 : 0;
+    }
+}
+
+// W1 = U + dt R1 / V (stage 2 input), with the stage-2 dt bookkeeping.
+template <class A>
+__global__ void __launch_bounds__(256) form_w1_kernel(GridParams gp, StageArgs sa, double *W1)
+{
+    const StepScalars sc = step_scalars<A, STAGE_2>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && sc.active) sa.ctrl->dt = sc.dt;
+    if (!sc.active) return;
+    const long long n = gp.plane;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)A::NVAR * n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long o = (long long)A::field((int)(i / n)) * n + i % n;
+        const double u = __ldg(sa.U + o), r = __ldg(sa.R + o);
+        W1[o] = IsExact<A>::value ? u + sc.dt * r / gp.vol : fma(sc.s, r, u);
+    }
+}
+
+// ---- face-side records ----------------------------------------------------
+// The state a cell (or a ghost) presents on side (d, s) of its faces:
+// interior U + s sigma_d / 2 (reconstruction eval, oracle eval_side); a ghost
+// across the border of direction d shows the ghost of the neighbouring
+// interior cell's face state (euler.cpp:224-225).
+template <class A, int DIM>
+struct SideRec {
+    CellRecV<1, A::NVAR> r[DIM][2];   // [direction][side: 0 = -e_d, 1 = +e_d]
+};
+
+// Record for one face side: record() on a face state, keeping direction d only.
+template <class A, int DIM>
+__device__ __forceinline__ void side_record(const double *c, int d, CellRecV<1, A::NVAR> &out, unsigned *status)
+{
+    CellRecV<DIM, A::NVAR> full;
+#pragma unroll
+    for (int k = 0; k < A::NVAR; ++k) full.c[k] = c[k];
+    A::template record<DIM>(full, status);
+#pragma unroll
+    for (int k = 0; k < A::NVAR; ++k) { out.c[k] = full.c[k]; out.f[0][k] = full.f[d][k]; }
+    out.lam[0] = full.lam[d];
+}
+
+// Face-side records of the cell at (x, y, z), which may be a ghost position.
+template <class A, int DIM>
+__device__ __forceinline__ void load_sides(const GridParams &gp, const double *state, const double *S, int x, int y,
+                                           int z, SideRec<A, DIM> &sr, unsigned *status)
+{
+    constexpr int NV = A::NVAR;
+    int gx, gy, gz = 0;
+    const int ix = resolve_index(x, gp.n[0], gp.bc_lo[0] == BC_PERIODIC, gx);
+    const int iy = resolve_index(y, gp.n[1], gp.bc_lo[1] == BC_PERIODIC, gy);
+    const int iz = (DIM == 3) ? resolve_index(z, gp.n[2], gp.bc_lo[2] == BC_PERIODIC, gz) : 0;
+    const long long n = gp.plane;
+    const long long g = (long long)ix + (long long)gp.n[0] * ((long long)iy + (long long)gp.n[1] * iz);
+    double uc[NV], sg[DIM][NV];
+    load_plain<A>(state, n, g, uc);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sg[d][k] = __ldg(S + (long long)(d * NV + k) * n + g);
+    const int gh[3] = {gx, gy, gz};
+    int gdir = -1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) if (gh[d] != 0 && gdir < 0) gdir = d;
+    if (gdir < 0) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                double fs[NV];
+                const double off = s ? 0.5 : -0.5;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) fs[k] = uc[k] + off * sg[d][k];
+                side_record<A, DIM>(fs, d, sr.r[d][s], s == 1 ? status : nullptr);
+            }
+        return;
+    }
+    // ghost across the border of direction gdir on side gh[gdir]: the face it
+    // shares with the interior cell is on its side -gh[gdir]; the interior
+    // face state is on the interior cell's side gh[gdir]
+    double fs[NV], gs[NV];
+    const double off = gh[gdir] > 0 ? 0.5 : -0.5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) fs[k] = uc[k] + off * sg[gdir][k];
+    double nrm[3] = {0.0, 0.0, 0.0};
+    nrm[gdir] = (double)gh[gdir];
+    ghost_state<A>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], nrm, fs, gp.dir_prim, gs);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) side_record<A, DIM>(gs, d, sr.r[d][s], nullptr);
+}
+
+template <class A>
+__device__ __forceinline__ double side_face(const CellRecV<1, A::NVAR> &L, const CellRecV<1, A::NVAR> &R, double *F)
+{
+    return A::face(L.c, L.f[0], L.lam[0], R.c, R.f[0], R.lam[0], F);
+}
+
+// x faces of a warp row from the +x record of each lane and the -x record of the next lane
+template <class A>
+__device__ __forceinline__ double xfaces_o2(const CellRecV<1, A::NVAR> &plus, const CellRecV<1, A::NVAR> &minus,
+                                            double *Flo, double *Fhi)
+{
+    constexpr int NV = A::NVAR;
+    CellRecV<1, NV> R;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { R.c[k] = shfl_down(minus.c[k], 1); R.f[0][k] = shfl_down(minus.f[0][k], 1); }
+    R.lam[0] = shfl_down(minus.lam[0], 1);
+    const double lam = side_face<A>(plus, R, Fhi);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) Flo[k] = shfl_up(Fhi[k], 1);
+    return lam;
+}
+
+// Output of one cell: stage state from the materialised planes.
+template <class A, int STAGE>
+__device__ __forceinline__ void store_output_o2(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                                const double *state, long long g, const double *acc)
+{
+#pragma unroll
+    for (int k = 0; k < A::NVAR; ++k) {
+        const long long o = (long long)A::field(k) * gp.plane + g;
+        const double cs = __ldg(state + o);
+        double v;
+        if (STAGE == STAGE_RHS || STAGE == STAGE_1) {
+            v = acc[k];
+        } else if (STAGE == STAGE_2) {
+            const double u = __ldg(sa.U + o);
+            if (IsExact<A>::value) v = 0.75 * u + 0.25 * (cs + sc.dt * acc[k] / gp.vol);
+            else v = fma(0.25, fma(sc.s, acc[k], cs), 0.75 * u);
+        } else {
+            const double u = sa.U[o];
+            if (IsExact<A>::value) v = (1. / 3) * u + (2. / 3) * (cs + sc.dt * acc[k] / gp.vol);
+            else v = fma(2.0 / 3.0, fma(sc.s, acc[k], cs), u * (1.0 / 3.0));
+        }
+        sa.out[o] = v;
+    }
+}
+
+// ---------------------------------------------------------------- 2D, order 2
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArgs sa, const double *state,
+                                                         const double *S)
+{
+    constexpr int NV = A::NVAR;
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (warp >= gp.nseg * gp.nchunk) return;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+
+    const int nx = gp.n[0], ny = gp.n[1];
+    const int seg = warp % gp.nseg, chunk = warp / gp.nseg;
+    const int x = seg * SEG - 1 + lane;
+    const int y0 = chunk * gp.chunk;
+    const int y1 = min(y0 + gp.chunk, ny);
+    const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
+    const bool xface_valid = (lane <= SEG) && (x < nx);
+    const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC;
+    unsigned status = 0;
+    unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
+    double lmax = 0.0;
+
+    SideRec<A, 2> cur, abv;
+    double Fylo[NV], Fyhi[NV], Fxlo[NV], Fxhi[NV], acc[NV];
+    load_sides<A, 2>(gp, state, S, x, y0 - 1, 0, abv, nullptr);
+    load_sides<A, 2>(gp, state, S, x, y0, 0, cur, st);
+    {
+        const double l = side_face<A>(abv.r[1][1], cur.r[1][0], Fylo);
+        if (out_col) lmax = max_nonneg(lmax, l);
+    }
+    for (int y = y0; y < y1; ++y) {
+        const double lx = xfaces_o2<A>(cur.r[0][1], cur.r[0][0], Fxlo, Fxhi);
+        if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
+        accumulate_pair<A, true>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
+        load_sides<A, 2>(gp, state, S, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
+        const double ly = side_face<A>(cur.r[1][1], abv.r[1][0], Fyhi);
+        if (STAGE <= STAGE_1 && out_col) lmax = max_nonneg(lmax, ly);
+        if (out_col) {
+            accumulate_pair<A, false>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
+            store_output_o2<A, STAGE>(sa, gp, sc, state, (long long)x + (long long)nx * y, acc);
+        }
+        cur = abv;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fylo[k] = Fyhi[k];
+    }
+    if (STAGE <= STAGE_1) {
+        lmax = warp_max(lmax);
+        if (lane == 0) {
+            unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
+                                                           : &sa.ctrl->maxeig_bits;
+            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        }
+        if (STAGE == STAGE_1) {
+            status = __reduce_or_sync(0xffffffffu, status);
+            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- 3D, order 2
+template <int BY, int NV>
+struct Smem3DO2 {
+    double c[BY][NV][32];
+    double f[BY][NV][32];
+    double lam[BY][32];
+    double F[BY][NV][32];
+};
+
+template <class A, int STAGE, int BY>
+__global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, StageArgs sa, const double *state,
+                                                             const double *S)
+{
+    constexpr int NV = A::NVAR;
+    __shared__ Smem3DO2<BY, NV> sm;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    int b = blockIdx.x;
+    const int seg = b % gp.nseg; b /= gp.nseg;
+    const int rb = b % gp.nrowblk; b /= gp.nrowblk;
+    const int chunk = b;
+    const int x = seg * SEG - 1 + lane;
+    const int y = rb * (BY - 2) - 1 + w;
+    const int z0 = chunk * gp.chunk;
+    const int z1 = min(z0 + gp.chunk, nz);
+    const bool halo_lo = (w == 0), halo_hi = (w == BY - 1);
+    const bool out_row = !halo_lo && !halo_hi && (y < ny);
+    const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
+    const bool out = out_row && out_col;
+    const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
+               perz = gp.bc_lo[2] == BC_PERIODIC;
+    unsigned status = 0;
+    unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
+    double lmax = 0.0;
+
+    SideRec<A, 3> cur, abv;
+    double Fzlo[NV], Fzhi[NV], Fa[NV], Fb[NV], acc[NV];
+    if (!halo_lo && !halo_hi) {
+        load_sides<A, 3>(gp, state, S, x, y, z0 - 1, abv, nullptr);
+        load_sides<A, 3>(gp, state, S, x, y, z0, cur, st);
+        const double l = side_face<A>(abv.r[2][1], cur.r[2][0], Fzlo);
+        if (out) lmax = max_nonneg(lmax, l);
+    }
+    for (int z = z0; z < z1; ++z) {
+        if (halo_lo || halo_hi) {
+            SideRec<A, 3> h;
+            load_sides<A, 3>(gp, state, S, x, y, z, h, nullptr);
+            // the face side this halo row shows to the block: +y for the row below, -y above
+            const CellRecV<1, NV> &hr = halo_lo ? h.r[1][1] : h.r[1][0];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = hr.c[k]; sm.f[w][k][lane] = hr.f[0][k]; }
+            sm.lam[w][lane] = hr.lam[0];
+            __syncthreads();
+            if (halo_hi) {
+                CellRecV<1, NV> L;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { L.c[k] = sm.c[w - 1][k][lane]; L.f[0][k] = sm.f[w - 1][k][lane]; }
+                L.lam[0] = sm.lam[w - 1][lane];
+                const double ly = side_face<A>(L, hr, Fa);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.F[w][k][lane] = Fa[k];
+                if (STAGE <= STAGE_1 && out_col && y - 1 < ny) lmax = max_nonneg(lmax, ly);
+            }
+            __syncthreads();
+            __syncthreads();
+            continue;
+        }
+        const double lx = xfaces_o2<A>(cur.r[0][1], cur.r[0][0], Fa, Fb);
+        if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = max_nonneg(lmax, lx);
+        accumulate_pair<A, true>(acc, Fa, Fb, gp.area, perx && x == nx - 1);
+        // y faces: rows publish their +y side, each row evaluates the face below it
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = cur.r[1][1].c[k]; sm.f[w][k][lane] = cur.r[1][1].f[0][k]; }
+        sm.lam[w][lane] = cur.r[1][1].lam[0];
+        __syncthreads();
+        {
+            CellRecV<1, NV> L;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { L.c[k] = sm.c[w - 1][k][lane]; L.f[0][k] = sm.f[w - 1][k][lane]; }
+            L.lam[0] = sm.lam[w - 1][lane];
+            const double ly = side_face<A>(L, cur.r[1][0], Fa);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sm.F[w][k][lane] = Fa[k];
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fb[k] = sm.F[w + 1][k][lane];
+        accumulate_pair<A, false>(acc, Fa, Fb, gp.area, pery && y == ny - 1);
+        load_sides<A, 3>(gp, state, S, x, y, z + 1, abv, (z + 1 < z1) ? st : nullptr);
+        const double lz = side_face<A>(cur.r[2][1], abv.r[2][0], Fzhi);
+        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+        if (out) {
+            accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
+            store_output_o2<A, STAGE>(sa, gp, sc, state,
+                                      (long long)x + (long long)nx * ((long long)y + (long long)ny * z), acc);
+        }
+        __syncthreads();
+        cur = abv;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
+    }
+    if (STAGE <= STAGE_1) {
+        lmax = warp_max(lmax);
+        if (lane == 0) {
+            unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
+                                                           : &sa.ctrl->maxeig_bits;
+            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        }
+        if (STAGE == STAGE_1) {
+            status = __reduce_or_sync(0xffffffffu, status);
+            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
+        }
+    }
+}
+
+} // namespace mmf

@@ -177,6 +177,7 @@ class Case:
     max_steps: int = -1
     periodic: bool = False
     prm: Params = field(default_factory=Params)
+    border_bc: int = None     # overrides the problem's border condition (problem.cpp:404-420)
 
     @property
     def h(self):
@@ -189,7 +190,7 @@ class Case:
     def bcs(self):
         if self.periodic:
             return [BC_PERIODIC] * 3, [BC_PERIODIC] * 3
-        b = border_bc_type(self.problem)
+        b = border_bc_type(self.problem) if self.border_bc is None else self.border_bc
         return [b] * 3, [b] * 3
 
     def centroids(self):
@@ -198,10 +199,10 @@ class Case:
     def initial_state(self):
         return exact_conservatives(self.problem, self.dim, self.centroids(), 0.0, self.prm)
 
-    def solver(self, arith="fast", device=0, chunk=0):
+    def solver(self, arith="fast", device=0, chunk=0, order=1):
         from .solver import CartesianEuler
         lo, hi = self.bcs()
-        return CartesianEuler(self.dim, self.n, self.origin, self.h, lo, hi, order=1, arith=arith,
+        return CartesianEuler(self.dim, self.n, self.origin, self.h, lo, hi, order=order, arith=arith,
                               device=device, chunk=chunk)
 
     def l1_density_error(self, U, t):
@@ -226,7 +227,7 @@ def radial_sod_2d(n=1024, t_end=0.25, cfl=0.5, max_steps=-1):
     """Radial Sod on [-1,1]^2: rho=p=1 for r<0.5, rho=0.125, p=0.1 outside, transmissive borders."""
     prm = Params(sod_radius=0.5)
     return Case("radial_sod_2d_%d" % n, RADSOD, 2, (n, n, 1), (-1.0, -1.0, 0.0), 2.0, cfl, t_end=t_end,
-                max_steps=max_steps, prm=prm)
+                max_steps=max_steps, prm=prm, border_bc=BC_FREE_FLOW)
 
 
 def vortex(dim=2, n=64, axis="z", steps=100, cfl=0.5, beta=5.0, periodic=True):

@@ -106,9 +106,33 @@ class CartesianEuler:
         capi.check(self._lib.mmf_compute_rhs(self._ctx, capi.ptr(U), capi.ptr(R), C.byref(me), self.ncells))
         return R, me.value
 
-    def compute_polynomials(self):
-        """reconstruction::computePolynomials (reconstruction.cpp:47-55)."""
-        capi.check(self._lib.mmf_compute_polynomials(self._ctx))
+    def compute_polynomials(self, U=None, want_slopes=True, want_active=True):
+        """reconstruction::computePolynomials (reconstruction.cpp:47-55) of state U.
+
+        Order 1: nothing to compute (returns None).  Order 2: returns
+        (slopes [n_raw, 3, 5], limiter_active [n_raw] uint8)."""
+        if self.grid.order == 1:
+            capi.check(self._lib.mmf_compute_polynomials(self._ctx, None, None, None, self.ncells))
+            return None
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        S = np.empty((self.ncells, 3, 5)) if want_slopes else None
+        A = np.empty(self.ncells, dtype=np.uint8) if want_active else None
+        capi.check(self._lib.mmf_compute_polynomials(self._ctx, capi.ptr(U), capi.ptr(S), capi.ptr(A), self.ncells))
+        return S, A
+
+    def set_limiter(self, mode, flags=None):
+        """Order-2 limiter: 'all', 'none' or 'flagged' (flags: one byte per raw id)."""
+        m = {"all": capi.LIMIT_ALL, "none": capi.LIMIT_NONE, "flagged": capi.LIMIT_FLAGGED}.get(mode, mode)
+        f = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
+        capi.check(self._lib.mmf_set_limiter(self._ctx, m, capi.ptr(f), self.ncells))
+
+    def set_limiter_flags_device(self, d_flags_grid):
+        capi.check(self._lib.mmf_set_limiter_flags_device(self._ctx, capi.ptr(d_flags_grid)))
+
+    def limiter_activity(self):
+        a = np.empty(self.ncells, dtype=np.uint8)
+        capi.check(self._lib.mmf_get_limiter_activity(self._ctx, capi.ptr(a), self.ncells))
+        return a
 
     def time_setup(self, cfl, t=0.0, t_end=math.inf, max_steps=-1):
         capi.check(self._lib.mmf_time_setup(self._ctx, cfl, t, t_end, max_steps))

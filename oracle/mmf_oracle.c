@@ -319,6 +319,9 @@ int orc_mesh_build(orc_mesh *m, int problem, int dim, const int64_t *n, const do
     m->bc = malloc(nf * sizeof(int));
     m->fdir = malloc(nf * sizeof(int));
     const double area = (dim == 3) ? h * h : h;
+    /* border condition of each side as the faces resolve it (the ghost cells of
+     * the order-2 slopes use it) */
+    int side_bc_lo[3] = {-100, -100, -100}, side_bc_hi[3] = {-100, -100, -100};
     int64_t f = 0;
     for (int d = 0; d < dim; ++d) {
         int per = (m->bc_lo[d] == ORC_BC_PERIODIC);
@@ -348,11 +351,13 @@ int orc_mesh_build(orc_mesh *m, int problem, int dim, const int64_t *n, const do
                         m->owner[f] = m->raw_of_grid[ghi];
                         m->neigh[f] = -1;
                         m->bc[f] = (m->bc_lo[d] >= 0) ? m->bc_lo[d] : orc_border_bc_type(problem, fc);
+                        if (side_bc_lo[d] == -100) side_bc_lo[d] = m->bc[f];
                     } else if (!per && idx[d] == nd) {
                         nrm[d] = 1.0;
                         m->owner[f] = m->raw_of_grid[glo];
                         m->neigh[f] = -1;
                         m->bc[f] = (m->bc_hi[d] >= 0) ? m->bc_hi[d] : orc_border_bc_type(problem, fc);
+                        if (side_bc_hi[d] == -100) side_bc_hi[d] = m->bc[f];
                     } else {
                         nrm[d] = 1.0;
                         m->owner[f] = m->raw_of_grid[glo];
@@ -367,8 +372,8 @@ int orc_mesh_build(orc_mesh *m, int problem, int dim, const int64_t *n, const do
     }
     /* record the resolved border BCs */
     for (int d = 0; d < 3; ++d) {
-        if (m->bc_lo[d] < 0) m->bc_lo[d] = (d < dim) ? ORC_BC_FREE_FLOW : -1;
-        if (m->bc_hi[d] < 0) m->bc_hi[d] = (d < dim) ? ORC_BC_FREE_FLOW : -1;
+        if (m->bc_lo[d] < 0) m->bc_lo[d] = (d < dim && side_bc_lo[d] != -100) ? side_bc_lo[d] : -1;
+        if (m->bc_hi[d] < 0) m->bc_hi[d] = (d < dim && side_bc_hi[d] != -100) ? side_bc_hi[d] : -1;
     }
     return 0;
 }

@@ -42,7 +42,7 @@ def _grid(mmf, **kw):
 
 
 @pytest.mark.parametrize("kw,code", [
-    (dict(dim=4), -1), (dict(h=0.0), -1), (dict(n=[0, 8, 1]), -1), (dict(order=2), -4),
+    (dict(dim=4), -1), (dict(h=0.0), -1), (dict(n=[0, 8, 1]), -1), (dict(order=3), -4),
     (dict(bc_lo=[16, 0, 0], bc_hi=[0, 0, 0]), -1), (dict(bc_lo=[7, 0, 0]), -1), (dict(arith=5), -1)])
 def test_create_rejects_bad_arguments(mmf, kw, code):
     lib = mmf.capi.load()

@@ -26,9 +26,8 @@ def rel_err(a, b):
 
 
 def oracle_mesh(orc, case, cell_order=0):
-    P = orc.BC_PERIODIC
-    lo = [P] * 3 if case.periodic else None
-    return orc.OracleMesh(case.problem, case.dim, case.n, case.origin, case.length, bc_lo=lo, bc_hi=lo,
+    lo, hi = case.bcs()
+    return orc.OracleMesh(case.problem, case.dim, case.n, case.origin, case.length, bc_lo=lo, bc_hi=hi,
                           cell_order=cell_order)
 
 
