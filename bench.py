@@ -169,6 +169,75 @@ def cpu_baseline(n, seconds, procs):
 
 
 # ---------------------------------------------------------------- GPU arm
+def run_batched(args, world, rank, local, dist):
+    """512 uneven 2D cases (seeded) in one persistent launch per stage; the plain
+    reference point runs the same cases one after another with single-case
+    contexts (16-step graphs each)."""
+    import torch
+    import minimmerflow_gb300 as mmf
+    from minimmerflow_gb300.batch import BatchEuler
+
+    torch.cuda.set_device(local)
+    cases = mmf.problem.batched_sweep(ncases=args.ncases, seed=args.seed)
+    states = [c.initial_state() for c in cases]
+    b = BatchEuler(cases, arith=args.arith, device=local)
+    b.upload(states)
+    horizon = args.warmup + args.steps + 64
+    b.time_setup(max_steps=horizon)
+    chunk, bps = b.autotune(trial_steps=2)
+    stream = torch.cuda.ExternalStream(b.stream_handle, device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    b.advance_async(args.warmup)
+    b.synchronize()
+    launches0 = b.launch_count
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    durs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.advance_async(1)
+        e1.record(stream)
+        e1.synchronize()
+        durs.append(e0.elapsed_time(e1) / 1e3)
+    clocks = clk.stop()
+    launches = b.launch_count - launches0
+    total = sum(durs)
+    if dist is not None:
+        tt = torch.tensor([total], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total = float(tt.item())
+    value = world * b.total * args.steps / total
+    status_bad = sum(1 for i in range(len(cases)) if b.case_info(i)[2])
+    b.close()
+    # plain: single-case contexts one after another
+    k_plain = max(2, min(args.steps, 8))
+    ctxs = []
+    for c, U0 in zip(cases, states):
+        s = c.solver(arith=args.arith, device=local)
+        s.upload(U0)
+        s.time_setup(c.cfl, 0.0, math.inf, 10 ** 9)
+        s.advance(1)
+        ctxs.append(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in ctxs:
+        s.advance(k_plain)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_value = sum(c.ncells for c in cases) * k_plain / plain_s
+    for s in ctxs:
+        s.close()
+    return dict(value=value, total=total, clocks=clocks, launches=launches, ncell=b.total, chunk=chunk, bps=bps,
+                plain=plain_value, status_bad=status_bad, ncases=len(cases))
+
+
 def make_case(args):
     import minimmerflow_gb300 as mmf
     if args.workload == "sod2d":
@@ -180,6 +249,12 @@ def make_case(args):
 
 
 def workload_config(args, world):
+    if args.workload == "batched":
+        return {"workload": ("batched sweep: %d independent 2D cases (seed %d), side U{32..512}, half isentropic "
+                             "vortices beta~U[1,8] (periodic [-5,5]^2), half radial Sods p-ratio logU[2,100], "
+                             "rho-ratio U[2,10] (transmissive [-1,1]^2), CFL 0.5 per case, order 1, FP64"
+                             % (args.ncases, args.seed)),
+                "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
     if args.workload == "sod2d":
         w = "2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, to t=0.25, order 1, FP64" % (args.n, args.n)
         cells = args.n * args.n
@@ -302,7 +377,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
-    ap.add_argument("--workload", default="sod2d", choices=["sod2d", "vortex3d_z", "vortex3d_x"])
+    ap.add_argument("--workload", default="sod2d", choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched"])
+    ap.add_argument("--ncases", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--order", type=int, default=1, choices=[1, 2])
@@ -332,6 +409,25 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.workload == "batched":
+        r = run_batched(args, world, rank, local, dist)
+        if rank != 0:
+            return
+        hbm_peak, peak_src = read_peaks()
+        line = {"metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(workload, cells=r["ncell"], autotuned_chunk=r["chunk"], blocks_per_sm=r["bps"]),
+                "arith": args.arith,
+                "roofline": {"bound": "hbm", "kernel": "stage2d_batch_kernel (3 per step)",
+                             "achieved": CELL_BYTES_STEP * r["value"] / world / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": CELL_BYTES_STEP * r["value"] / world / 1e9 / hbm_peak, "peak_source": peak_src,
+                             "traffic": None},
+                "plain_single_case_contexts": {"value": r["plain"], "unit": metric,
+                                               "how": "same cases, one context each, run one after another"},
+                "clocks": r["clocks"], "gpu_launches": r["launches"], "cases_with_status": r["status_bad"]}
+        print(json.dumps(line))
+        return
     r = run_ours(args, world, rank, local, dist)
     if rank != 0:
         return

@@ -157,6 +157,35 @@ int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, co
 int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
                        const double *dirichlet_prim, double *cons_bc);
 
+/* ---- batched cases ------------------------------------------------------ */
+/* Many independent 2D order-1 cases of uneven size advanced together: one
+ * persistent launch per RK stage walks a list of (case, segment, row chunk)
+ * work items, each case keeps its own t, CFL dt (per-case maxEig reduction),
+ * step count and status, and the step sequence replays from a CUDA graph.
+ * Each case gets exactly the result of its own single-case context.  No
+ * reference counterpart (the reference runs one case per process). */
+typedef struct mmf_batch mmf_batch;
+int mmf_batch_create(int ncases, const mmf_grid *grids, int device, mmf_batch **out);
+int mmf_batch_destroy(mmf_batch *batch);
+int64_t mmf_batch_cell_count(const mmf_batch *batch);
+int64_t mmf_batch_launch_count(const mmf_batch *batch);
+void *mmf_batch_get_stream(mmf_batch *batch);
+/* all cases' states, AoS [total][5], case after case, each row-major */
+int mmf_batch_upload(mmf_batch *batch, const double *aos, int64_t total);
+int mmf_batch_download(mmf_batch *batch, double *aos, int64_t total);
+/* per-case CFL and end time (t_end NULL = no end time, then max_steps >= 0) */
+int mmf_batch_time_setup(mmf_batch *batch, const double *cfl, const double *t_end, int64_t max_steps);
+int mmf_batch_advance_async(mmf_batch *batch, int64_t n_steps);
+int mmf_batch_synchronize(mmf_batch *batch);
+int mmf_batch_case_info(mmf_batch *batch, int c, double *t, int64_t *steps, unsigned *status);
+/* Decomposition: rows per work item and resident blocks per SM (0 = occupancy maximum). */
+int mmf_batch_set_shape(mmf_batch *batch, int chunk, int blocks_per_sm);
+int mmf_batch_get_shape(mmf_batch *batch, int *chunk, int *blocks_per_sm);
+/* Times trial_steps steps per candidate shape (chunk in {8,16,32,64} x up to
+ * three block counts), keeps the fastest, restores the state; results are
+ * cached per workload signature for the process. */
+int mmf_batch_autotune(mmf_batch *batch, int trial_steps, int *chunk, int *blocks_per_sm);
+
 /* ---- residual without device allocation ------------------------------- */
 /* Largest mesh accepted by mmf_compute_rhs_noalloc. */
 #define MMF_NOALLOC_MAX_CELLS 65536

@@ -22,6 +22,10 @@ EXPORTS = [
     "mmf_rk_stage", "mmf_cons2prim", "mmf_prim2cons", "mmf_eval_fluxes", "mmf_eval_splitting",
     "mmf_eval_bc_values", "mmf_newton_selftest", "mmf_compute_rhs_noalloc", "mmf_set_limiter",
     "mmf_set_limiter_flags_device", "mmf_get_limiter_activity",
+    "mmf_batch_create", "mmf_batch_destroy", "mmf_batch_cell_count", "mmf_batch_launch_count",
+    "mmf_batch_get_stream", "mmf_batch_upload", "mmf_batch_download", "mmf_batch_time_setup",
+    "mmf_batch_advance_async", "mmf_batch_synchronize", "mmf_batch_case_info", "mmf_batch_set_shape",
+    "mmf_batch_get_shape", "mmf_batch_autotune",
 ]
 LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
@@ -84,6 +88,23 @@ def load(build_if_missing=True):
     L.mmf_eval_splitting.argtypes = [C.c_int64, _P, _P, _P, _P, _P]
     L.mmf_eval_bc_values.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P]
     L.mmf_newton_selftest.argtypes = [C.c_int64, _P, _P, _P]
+    L.mmf_batch_create.argtypes = [C.c_int, C.POINTER(Grid), C.c_int, C.POINTER(_P)]
+    L.mmf_batch_destroy.argtypes = [_P]
+    L.mmf_batch_cell_count.argtypes = [_P]
+    L.mmf_batch_cell_count.restype = C.c_int64
+    L.mmf_batch_launch_count.argtypes = [_P]
+    L.mmf_batch_launch_count.restype = C.c_int64
+    L.mmf_batch_get_stream.argtypes = [_P]
+    L.mmf_batch_get_stream.restype = C.c_void_p
+    L.mmf_batch_upload.argtypes = [_P, _P, C.c_int64]
+    L.mmf_batch_download.argtypes = [_P, _P, C.c_int64]
+    L.mmf_batch_time_setup.argtypes = [_P, _P, _P, C.c_int64]
+    L.mmf_batch_advance_async.argtypes = [_P, C.c_int64]
+    L.mmf_batch_synchronize.argtypes = [_P]
+    L.mmf_batch_case_info.argtypes = [_P, C.c_int, _D, C.POINTER(C.c_int64), C.POINTER(C.c_uint)]
+    L.mmf_batch_set_shape.argtypes = [_P, C.c_int, C.c_int]
+    L.mmf_batch_get_shape.argtypes = [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mmf_batch_autotune.argtypes = [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.mmf_compute_rhs_noalloc.argtypes = [C.POINTER(Grid), _P, _P, _P, _P, _P]
     _lib = L
     return L

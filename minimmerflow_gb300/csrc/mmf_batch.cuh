@@ -1,0 +1,86 @@
+// mmf_batch.cuh -- many independent 2D cases of uneven size in one persistent
+// launch per Runge-Kutta stage.
+//
+// The cases' states are packed field-plane by field-plane: field k of case c
+// is at base + k * total + offset_c, row-major inside the case.  The work of
+// a stage is a flat list of items, one per (case, 30-column segment, row
+// chunk), in case order; the persistent grid (a few blocks per SM) walks the
+// list warp by warp.  Each case keeps its own control block (time, dt, maxEig,
+// step, status), so dt is a per-case CFL reduction: a stage-1 item reduces its
+// maxEig into its case's slot, stage-2 items derive their case's dt from it,
+// and the first item of a case does that case's per-launch bookkeeping.  The
+// arithmetic of an item is the single-grid march (march2d), so every case
+// gets exactly the result it would get alone.
+#pragma once
+
+#include "mmf_cartesian.cuh"
+
+namespace mmf {
+
+struct CaseDesc {
+    GridParams gp;        // grid of the case (gp.plane = field stride of the packed planes)
+    long long offset;     // first cell of the case in the packed planes
+    int item0;            // first work item of the case
+    int pad;
+};
+
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_batch_kernel(const CaseDesc *__restrict__ cases,
+                                                            const int *__restrict__ item_case, int nitems,
+                                                            Ctrl *cctrl, StageArgs base)
+{
+    const int warp0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    for (int item = warp0; item < nitems; item += nwarps) {
+        const int c = item_case[item];
+        const GridParams gp = cases[c].gp;
+        const long long off = cases[c].offset;
+        const int local = item - cases[c].item0;
+        Ctrl *ctrl = cctrl + c;
+        const StepScalars sc = step_scalars<A, STAGE>(gp, ctrl);
+        if (local == 0 && lane == 0) step_bookkeeping<STAGE>(ctrl, sc);
+        if (!sc.active) continue;
+        StageArgs sa = base;
+        sa.U = base.U + off;
+        sa.R = base.R + off;
+        sa.W = base.W + off;
+        sa.out = base.out + off;
+        sa.ctrl = ctrl;
+        double lmax = 0.0;
+        unsigned status = 0;
+        march2d<A, STAGE>(gp, sa, sc, local % gp.nseg, local / gp.nseg, lmax, status);
+        publish_reductions<STAGE>(lmax, status, ctrl, nullptr);
+    }
+}
+
+template <class A>
+inline cudaError_t launch_batch(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                                const StageArgs &base, int blocks, cudaStream_t s)
+{
+    switch (stage) {
+    case STAGE_1: stage2d_batch_kernel<A, STAGE_1><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base); break;
+    case STAGE_2: stage2d_batch_kernel<A, STAGE_2><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base); break;
+    case STAGE_3: stage2d_batch_kernel<A, STAGE_3><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaPeekAtLastError();
+}
+
+template <class A>
+inline int batch_blocks_per_sm()
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stage2d_batch_kernel<A, STAGE_2>, 128, 0) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
+
+// Entry points (arithmetic translation units).
+cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                               const StageArgs &base, int blocks, cudaStream_t s);
+cudaError_t launch_batch_fast(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                              const StageArgs &base, int blocks, cudaStream_t s, bool w_zero);
+int batch_max_blocks_per_sm(int arith, bool w_zero);
+
+} // namespace mmf

@@ -281,27 +281,23 @@ __device__ __forceinline__ double xfaces(const RecOf<A, DIM> &r, double *Flo, do
 }
 
 // ---------------------------------------------------------------- 2D kernel
+// One warp's work item: 30 output columns (segment 'seg') over the rows of
+// chunk 'chunk' of the grid described by gp; sa holds the grid's planes
+// (field stride gp.plane).  Returns the item's maximum face eigenvalue (stage
+// 1 / residual only) and its status bits.
 template <class A, int STAGE>
-__global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs sa)
+__device__ __forceinline__ void march2d(const GridParams &gp, const StageArgs &sa, const StepScalars &sc, int seg,
+                                        int chunk, double &lmax, unsigned &status)
 {
     const int lane = threadIdx.x & 31;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (warp >= gp.nseg * gp.nchunk) return;
-    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
-    if (!sc.active) return;
-
     const int nx = gp.n[0], ny = gp.n[1];
-    const int seg = warp % gp.nseg, chunk = warp / gp.nseg;
     const int x = seg * SEG - 1 + lane;
     const int y0 = chunk * gp.chunk;
     const int y1 = min(y0 + gp.chunk, ny);
     const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
     const bool xface_valid = (lane <= SEG) && (x < nx);
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC;
-    unsigned status = 0;
     unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
-    double lmax = 0.0;
 
     constexpr int NV = A::NVAR;
     RecOf<A, 2> cur, abv;
@@ -329,17 +325,37 @@ __global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs s
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fylo[k] = Fyhi[k];
     }
-    if (STAGE <= STAGE_1) {
-        lmax = warp_max(lmax);
-        if (lane == 0) {
-            unsigned long long* dst = (STAGE == STAGE_RHS) ? (unsigned long long*)sa.rhs_maxeig : &sa.ctrl->maxeig_bits;
-            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
-        }
-        if (STAGE == STAGE_1) {
-            status = __reduce_or_sync(0xffffffffu, status);
-            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
-        }
+}
+
+// Warp-level publication of an item's max eigenvalue and status bits.
+template <int STAGE>
+__device__ __forceinline__ void publish_reductions(double lmax, unsigned status, Ctrl *ctrl, double *rhs_maxeig)
+{
+    if (STAGE > STAGE_1) return;
+    const int lane = threadIdx.x & 31;
+    lmax = warp_max(lmax);
+    if (lane == 0) {
+        unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)rhs_maxeig : &ctrl->maxeig_bits;
+        atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
     }
+    if (STAGE == STAGE_1) {
+        status = __reduce_or_sync(0xffffffffu, status);
+        if (lane == 0 && status) atomicOr(&ctrl->status, status);
+    }
+}
+
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs sa)
+{
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (warp >= gp.nseg * gp.nchunk) return;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+    double lmax = 0.0;
+    unsigned status = 0;
+    march2d<A, STAGE>(gp, sa, sc, warp % gp.nseg, warp / gp.nseg, lmax, status);
+    publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }
 
 // ---------------------------------------------------------------- 3D kernel

@@ -2,6 +2,7 @@
 // the pointwise kernels of the reference's unit-level functions.  Built with
 // -fmad=false so no multiply-add is contracted: the results are the
 // reference's CPU results bit for bit.
+#include "mmf_batch.cuh"
 #include "mmf_launch.cuh"
 
 namespace mmf {
@@ -15,6 +16,14 @@ cudaError_t launch_o2_exact(int op, int stage, const GridParams &gp, const Stage
                             double *W1, cudaStream_t s)
 {
     return launch_o2<ExactArith>(op, stage, gp, sa, oa, W1, s);
+}
+
+int batch_max_blocks_per_sm_exact() { return batch_blocks_per_sm<ExactArith>(); }
+
+cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                               const StageArgs &base, int blocks, cudaStream_t s)
+{
+    return launch_batch<ExactArith>(stage, cases, item_case, nitems, cctrl, base, blocks, s);
 }
 
 // One thread per item; arrays are AoS [n][5] (normals [n][3]).

@@ -1,5 +1,7 @@
 // mmf_fast.cu -- fast-arithmetic instantiation of the stage kernels (FMA
 // contraction on; one division and one square root per cell).
+#include "mmf_batch.cuh"
+#include "mmf_exact_occupancy.h"
 #include "mmf_launch.cuh"
 
 namespace mmf {
@@ -15,6 +17,19 @@ cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageA
 {
     if (gp.dim == 2 && w_zero) return launch_o2<FastArith2DW0, false>(op, stage, gp, sa, oa, W1, s);
     return launch_o2<FastArith>(op, stage, gp, sa, oa, W1, s);
+}
+
+cudaError_t launch_batch_fast(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                              const StageArgs &base, int blocks, cudaStream_t s, bool w_zero)
+{
+    if (w_zero) return launch_batch<FastArith2DW0>(stage, cases, item_case, nitems, cctrl, base, blocks, s);
+    return launch_batch<FastArith>(stage, cases, item_case, nitems, cctrl, base, blocks, s);
+}
+
+int batch_max_blocks_per_sm(int arith, bool w_zero)
+{
+    if (arith == 0) return batch_max_blocks_per_sm_exact();
+    return w_zero ? batch_blocks_per_sm<FastArith2DW0>() : batch_blocks_per_sm<FastArith>();
 }
 
 __global__ void newton_selftest_kernel(long long n, const double *x, double *r, double *q)

@@ -237,3 +237,34 @@ def vortex(dim=2, n=64, axis="z", steps=100, cfl=0.5, beta=5.0, periodic=True):
     prm = Params(vortex_beta=beta, periodic=periodic, origin=origin, length=10.0)
     return Case("vortex_%dd_%d_%s" % (dim, n, axis), prob, dim, (n, n, n if dim == 3 else 1), origin, 10.0,
                 cfl, max_steps=steps, periodic=periodic, prm=prm)
+
+
+def radial_sod_ratios(n, p_ratio, rho_ratio, cfl=0.5, max_steps=-1):
+    """[-1,1]^2 radial Sod, r < 0.5: rho = p = 1 inside, p = 1/p_ratio and
+    rho = 1/rho_ratio outside, transmissive borders."""
+    prm = Params(sod_radius=0.5, sod_rho_in=1.0, sod_p_in=1.0, sod_rho_out=1.0 / rho_ratio,
+                 sod_p_out=1.0 / p_ratio)
+    return Case("sod_p%.3g_r%.3g_%d" % (p_ratio, rho_ratio, n), RADSOD, 2, (n, n, 1), (-1.0, -1.0, 0.0), 2.0, cfl,
+                max_steps=max_steps, prm=prm, border_bc=BC_FREE_FLOW)
+
+
+def batched_sweep(ncases=512, seed=20261203, side_min=32, side_max=512, steps=-1):
+    """Independent 2D cases of uneven size from a seed: mesh side uniform in
+    [side_min, side_max]; even-indexed cases are isentropic vortices with beta
+    ~ U[1, 8] ([-5,5]^2, periodic), odd-indexed ones radial Sods with pressure
+    ratio ~ log-U[2, 100] and density ratio ~ U[2, 10]; CFL 0.5."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for i in range(ncases):
+        n = int(rng.integers(side_min, side_max + 1))
+        if i % 2 == 0:
+            beta = float(rng.uniform(1.0, 8.0))
+            c = vortex(2, n, steps=steps, beta=beta)
+            c.name = "vortex_b%.3g_%d" % (beta, n)
+        else:
+            pr = float(np.exp(rng.uniform(np.log(2.0), np.log(100.0))))
+            rr = float(rng.uniform(2.0, 10.0))
+            c = radial_sod_ratios(n, pr, rr, max_steps=steps)
+        c.t_end = math.inf
+        cases.append(c)
+    return cases
