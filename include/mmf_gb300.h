@@ -186,6 +186,44 @@ int mmf_batch_get_shape(mmf_batch *batch, int *chunk, int *blocks_per_sm);
  * cached per workload signature for the process. */
 int mmf_batch_autotune(mmf_batch *batch, int trial_steps, int *chunk, int *blocks_per_sm);
 
+/* ---- learned troubled-cell indicator (order 2) --------------------------- */
+/* A small MLP predicts, from the normalised primitive variables of a cell's
+ * 3^dim stencil (dim 2: 45 inputs padded to 48; dim 3: 135 padded to 144),
+ * whether the order-2 limiter would change one of the cell's slopes; cells
+ * predicted smooth take central slopes and skip the limiter.  135 -> 64 ->
+ * 64 -> 1, GELU, sigmoid; BF16 operands, FP32 accumulation.  Training and
+ * inference run on the GPU (mma.sync BF16 training kernels, a fused tcgen05
+ * inference kernel).  No reference counterpart (the reference has no limiter). */
+typedef struct mmf_mlp mmf_mlp;
+int mmf_mlp_create(int dim, uint64_t seed, int device, mmf_mlp **out);
+int mmf_mlp_destroy(mmf_mlp *mlp);
+int64_t mmf_mlp_num_params(const mmf_mlp *mlp);
+/* Feature width KPAD of one sample (48 in 2D, 144 in 3D). */
+int mmf_mlp_input_width(const mmf_mlp *mlp);
+/* FP32 parameters W1 [64][KPAD], b1 [64], W2 [64][64], b2 [64], w3 [64], b3 */
+int mmf_mlp_get_params(mmf_mlp *mlp, float *params, int64_t n);
+int mmf_mlp_set_params(mmf_mlp *mlp, const float *params, int64_t n);
+/* Gradients of the mean binary cross-entropy over a batch (device features
+ * d_X: BF16 [B][KPAD]; d_y: labels 0/1; B a multiple of 16), to host memory. */
+int mmf_mlp_gradients(mmf_mlp *mlp, const void *d_X, const unsigned char *d_y, int64_t B, float *grad, float *loss);
+/* One Adam step on a batch. */
+int mmf_mlp_train_batch(mmf_mlp *mlp, const void *d_X, const unsigned char *d_y, int64_t B, float lr, float *loss);
+/* Probabilities of n stored samples (device in, device out). */
+int mmf_mlp_predict(mmf_mlp *mlp, const void *d_X, int64_t n, float *d_prob);
+/* Features of every cell of the uploaded state, grid order, into device
+ * memory d_X (BF16 [n][KPAD]). */
+int mmf_features(mmf_ctx *ctx, void *d_X);
+/* Training labels of the uploaded state: 1 where the order-2 limiter (every
+ * cell limited, reference arithmetic) changes a slope, grid order, device memory. */
+int mmf_limiter_labels(mmf_ctx *ctx, unsigned char *d_labels);
+/* Runs the indicator on the uploaded state: the limiter becomes
+ * MMF_LIMIT_FLAGGED with flag = (probability > threshold).  prob / flags
+ * (host, raw order, nullable) receive the probabilities and flags. */
+int mmf_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold, float *prob, unsigned char *flags);
+/* From the next step on, every step starts with the indicator on U (inside
+ * the step's CUDA graph); mlp = NULL switches it off (limiter back to ALL). */
+int mmf_set_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold);
+
 /* ---- residual without device allocation ------------------------------- */
 /* Largest mesh accepted by mmf_compute_rhs_noalloc. */
 #define MMF_NOALLOC_MAX_CELLS 65536

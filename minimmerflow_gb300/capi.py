@@ -26,6 +26,9 @@ EXPORTS = [
     "mmf_batch_get_stream", "mmf_batch_upload", "mmf_batch_download", "mmf_batch_time_setup",
     "mmf_batch_advance_async", "mmf_batch_synchronize", "mmf_batch_case_info", "mmf_batch_set_shape",
     "mmf_batch_get_shape", "mmf_batch_autotune",
+    "mmf_mlp_create", "mmf_mlp_destroy", "mmf_mlp_num_params", "mmf_mlp_input_width", "mmf_mlp_get_params",
+    "mmf_mlp_set_params", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
+    "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
 ]
 LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
@@ -105,6 +108,20 @@ def load(build_if_missing=True):
     L.mmf_batch_set_shape.argtypes = [_P, C.c_int, C.c_int]
     L.mmf_batch_get_shape.argtypes = [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.mmf_batch_autotune.argtypes = [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mmf_mlp_create.argtypes = [C.c_int, C.c_uint64, C.c_int, C.POINTER(_P)]
+    L.mmf_mlp_destroy.argtypes = [_P]
+    L.mmf_mlp_num_params.argtypes = [_P]
+    L.mmf_mlp_num_params.restype = C.c_int64
+    L.mmf_mlp_input_width.argtypes = [_P]
+    L.mmf_mlp_get_params.argtypes = [_P, _P, C.c_int64]
+    L.mmf_mlp_set_params.argtypes = [_P, _P, C.c_int64]
+    L.mmf_mlp_gradients.argtypes = [_P, _P, _P, C.c_int64, _P, C.POINTER(C.c_float)]
+    L.mmf_mlp_train_batch.argtypes = [_P, _P, _P, C.c_int64, C.c_float, C.POINTER(C.c_float)]
+    L.mmf_mlp_predict.argtypes = [_P, _P, C.c_int64, _P]
+    L.mmf_features.argtypes = [_P, _P]
+    L.mmf_indicator.argtypes = [_P, _P, C.c_float, _P, _P]
+    L.mmf_set_indicator.argtypes = [_P, _P, C.c_float]
+    L.mmf_limiter_labels.argtypes = [_P, _P]
     L.mmf_compute_rhs_noalloc.argtypes = [C.POINTER(Grid), _P, _P, _P, _P, _P]
     _lib = L
     return L

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/mmf_gb300.h"
 #include "mmf_launch.cuh"
@@ -70,6 +71,12 @@ __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__rest
 namespace mmf {
 // Records an error for mmf_last_error() from another translation unit.
 int set_last_error(int code, const char *msg) { return fail(code, msg); }
+// mmf_mlp.cu
+cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
+                          unsigned char *flags, cudaStream_t s);
+cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s);
+int mlp_dim(const mmf_mlp *p);
+int mlp_error(mmf_mlp *p);
 }
 
 struct mmf_ctx {
@@ -94,6 +101,8 @@ struct mmf_ctx {
     unsigned char *lim_flag = nullptr;  // per cell: limit (1) / central slope (0) in LIMIT_FLAGGED mode
     unsigned char *lim_active = nullptr;// per cell: the limiter changed a slope (stage 1 of the last step)
     int limit_mode = LIMIT_ALL;
+    mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
+    float ind_threshold = 0.5f;
 
     cudaError_t stage(int st, const double *U_in, double *out)
     {
@@ -125,6 +134,11 @@ struct mmf_ctx {
         if (grid.order == 2) {
             // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
             // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
+            if (indicator) {
+                ++launches;
+                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream)) != cudaSuccess)
+                    return e;
+            }
             if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
             if ((e = o2(O2_STAGE, STAGE_1, U, R, nullptr)) != cudaSuccess) return e;
             if ((e = o2(O2_FORM_W1, STAGE_2, U, W, nullptr)) != cudaSuccess) return e;
@@ -137,7 +151,7 @@ struct mmf_ctx {
         if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U, U);
     }
-    int launches_per_step() const { return grid.order == 2 ? 7 : 3; }
+    int launches_per_step() const { return grid.order == 2 ? (indicator ? 8 : 7) : 3; }
 };
 
 static int check_ctx(mmf_ctx *ctx)
@@ -465,6 +479,88 @@ int mmf_set_limiter_flags_device(mmf_ctx *c, const unsigned char *d_flags_grid)
     if (c->grid.order != 2 || !d_flags_grid) return fail(MMF_ERR_ARG, "order-2 context and flags required");
     MMF_CUDA(cudaMemcpyAsync(c->lim_flag, d_flags_grid, (size_t)c->gp.plane, cudaMemcpyDeviceToDevice, c->stream));
     c->limit_mode = LIMIT_FLAGGED;
+    return MMF_OK;
+}
+
+int mmf_features(mmf_ctx *c, void *d_X)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!d_X) return fail(MMF_ERR_ARG, "null feature buffer");
+    ++c->launches;
+    MMF_CUDA(mlp_features(c->grid.dim, c->gp, c->U, d_X, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold, float *prob, unsigned char *flags)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!mlp) return fail(MMF_ERR_ARG, "null MLP");
+    if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
+    if (mlp_dim(mlp) != c->grid.dim) return fail(MMF_ERR_ARG, "MLP dimension differs from the mesh");
+    const long long n = c->gp.plane;
+    float *dprob = nullptr;
+    if (prob) MMF_CUDA(cudaMalloc(&dprob, sizeof(float) * (size_t)n));
+    ++c->launches;
+    cudaError_t e = mlp_indicator(mlp, c->gp, c->U, threshold, dprob, c->lim_flag, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && mlp_error(mlp)) { cudaFree(dprob); return fail(MMF_ERR_CUDA, "indicator: a wait gave up"); }
+    if (e == cudaSuccess && prob) {
+        std::vector<float> tmp((size_t)n);
+        e = cudaMemcpy(tmp.data(), dprob, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) {
+            std::vector<long long> map((size_t)n);
+            if (c->raw_to_cell) e = cudaMemcpy(map.data(), c->raw_to_cell, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost);
+            for (long long r = 0; r < n && e == cudaSuccess; ++r) prob[r] = tmp[(size_t)(c->raw_to_cell ? map[(size_t)r] : r)];
+        }
+    }
+    cudaFree(dprob);
+    MMF_CUDA(e);
+    c->limit_mode = LIMIT_FLAGGED;
+    if (flags) {
+        unsigned char *tmp = nullptr;
+        MMF_CUDA(cudaMalloc(&tmp, (size_t)n));
+        bytes_to_raw_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->lim_flag, tmp, n, c->raw_to_cell);
+        ++c->launches;
+        e = cudaPeekAtLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(flags, tmp, (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(tmp);
+        MMF_CUDA(e);
+    }
+    return MMF_OK;
+}
+
+int mmf_limiter_labels(mmf_ctx *c, unsigned char *d_labels)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the limiter applies to order 2");
+    if (!d_labels) return fail(MMF_ERR_ARG, "null label buffer");
+    // the reference-arithmetic limiter on every cell, on the uploaded state
+    const int saved = c->limit_mode;
+    c->limit_mode = LIMIT_ALL;
+    cudaError_t e = c->o2(O2_SLOPES, STAGE_RHS, c->U, nullptr, c->lim_active);
+    c->limit_mode = saved;
+    MMF_CUDA(e);
+    MMF_CUDA(cudaMemcpyAsync(d_labels, c->lim_active, (size_t)c->gp.plane, cudaMemcpyDeviceToDevice, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_set_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (mlp && c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
+    if (mlp && mlp_dim(mlp) != c->grid.dim) return fail(MMF_ERR_ARG, "MLP dimension differs from the mesh");
+    c->indicator = mlp;
+    c->ind_threshold = threshold;
+    c->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;
+    if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+    if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
     return MMF_OK;
 }
 

@@ -1,0 +1,324 @@
+// mmf_mlp.cuh -- learned troubled-cell indicator: a 3-layer MLP over the
+// normalised primitive variables of a cell's (3^dim)-cell stencil that
+// predicts where the order-2 limiter would change a slope, so that cells
+// predicted smooth take central slopes and skip the limiter.
+//
+//   features  x (dim 2: 9 x 5 = 45, padded to 48; dim 3: 27 x 5 = 135, padded
+//             to 144): for each primitive q in (rho, u, v, w, p), FP32,
+//             (q_j - q_c) / (max_j |q_j - q_c| + eps_q) over the stencil (c the
+//             centre cell; eps = 1e-4 |q_c| for rho and p, 1e-4 a_c for the
+//             velocities, a_c the centre sound speed); borders wrap (periodic)
+//             or clamp (zero gradient)
+//   network   h1 = GELU(W1 x + b1) (64), h2 = GELU(W2 h1 + b2) (64),
+//             y = sigmoid(w3 . h2 + b3); BF16 operands, FP32 accumulation
+//
+// Inference (mlp_infer_kernel) is one fused, persistent tcgen05 kernel per
+// 128-cell tile: the 128 threads of a CTA compute one cell's features each
+// and store them as BF16 in the shared-memory operand layout; one thread
+// issues tcgen05.mma into a TMEM accumulator (layer 1: 9 MMAs of K 16 for
+// 3D), the tile's h1 comes back with tcgen05.ld, goes through GELU into a
+// second shared operand, layer 2 accumulates into a second TMEM region, and
+// each thread finishes its own row (GELU, dot with w3, sigmoid).  Weights are
+// staged once per CTA with bulk asynchronous copies (cp.async.bulk).
+//
+// Shared operand layout (K-major, no swizzle): 8-row x 16-byte core matrices;
+// core matrix (row block rb, k block kb) at byte (kb * ROWS/8 + rb) * 128, row
+// r of it at r * 16.  Descriptor: leading byte offset = ROWS/8 * 128 (next
+// core matrix along K), stride byte offset = 128 (next 8-row block).
+//
+// Training runs on the GPU as well (mlp_train.cuh): forward, backward and Adam
+// kernels with mma.sync BF16 matmuls accumulated in FP32.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "mmf_cartesian.cuh"
+
+namespace mmf {
+
+constexpr int MLP_H = 64;            // hidden width
+constexpr int MLP_TILE = 128;        // cells per tcgen05 tile (M)
+
+__host__ __device__ constexpr int mlp_kin(int dim) { return dim == 3 ? 135 : 45; }
+__host__ __device__ constexpr int mlp_kpad(int dim) { return dim == 3 ? 144 : 48; }
+
+// Flat FP32 parameter vector: W1 [64][KPAD], b1 [64], W2 [64][64], b2 [64], w3 [64], b3 [1]
+__host__ __device__ constexpr long long mlp_off_b1(int dim) { return (long long)MLP_H * mlp_kpad(dim); }
+__host__ __device__ constexpr long long mlp_off_w2(int dim) { return mlp_off_b1(dim) + MLP_H; }
+__host__ __device__ constexpr long long mlp_off_b2(int dim) { return mlp_off_w2(dim) + MLP_H * MLP_H; }
+__host__ __device__ constexpr long long mlp_off_w3(int dim) { return mlp_off_b2(dim) + MLP_H; }
+__host__ __device__ constexpr long long mlp_off_b3(int dim) { return mlp_off_w3(dim) + MLP_H; }
+__host__ __device__ constexpr long long mlp_nparams(int dim) { return mlp_off_b3(dim) + 1; }
+
+// element offset of (row, k) in the K-major no-swizzle operand layout
+__host__ __device__ __forceinline__ int core_offset(int row, int k, int rows)
+{
+    return (((k >> 3) * (rows >> 3) + (row >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x)
+{
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * __expf(-0.5f * x * x);
+}
+__device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+// Primitive variables (rho, u, v, w, p) of the cell at (x, y, z), border wrap or clamp.
+__device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, int x, int y, int z, float *q)
+{
+    const bool px = gp.bc_lo[0] == BC_PERIODIC, py = gp.bc_lo[1] == BC_PERIODIC, pz = gp.bc_lo[2] == BC_PERIODIC;
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    x = x < 0 ? (px ? nx - 1 : 0) : (x >= nx ? (px ? 0 : nx - 1) : x);
+    y = y < 0 ? (py ? ny - 1 : 0) : (y >= ny ? (py ? 0 : ny - 1) : y);
+    z = z < 0 ? (pz ? nz - 1 : 0) : (z >= nz ? (pz ? 0 : nz - 1) : z);
+    const long long g = (long long)x + (long long)nx * ((long long)y + (long long)ny * z);
+    const long long n = gp.plane;
+    const float rho = (float)__ldg(U + g);
+    const float ri = 1.0f / rho;
+    const float u = (float)__ldg(U + n + g) * ri, v = (float)__ldg(U + 2 * n + g) * ri,
+                w = (float)__ldg(U + 3 * n + g) * ri;
+    const float E = (float)__ldg(U + 4 * n + g);
+    q[0] = rho;
+    q[1] = u;
+    q[2] = v;
+    q[3] = w;
+    q[4] = (float)(GAMMA - 1.0) * (E - 0.5f * rho * (u * u + v * v + w * w));
+}
+
+// The KPAD features of grid cell g (FP32), written through 'put(k, value)'.
+template <int DIM, class Put>
+__device__ __forceinline__ void cell_features(const double *U, const GridParams &gp, long long g, Put put)
+{
+    constexpr int NS = DIM == 3 ? 27 : 9;
+    const int nx = gp.n[0], ny = gp.n[1];
+    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = DIM == 3 ? (int)(g / ((long long)nx * ny)) : 0;
+    float q[NS][5];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
+        prim_at(U, gp, x + dx, y + dy, z + dz, q[s]);
+    }
+    constexpr int C = DIM == 3 ? 13 : 4;   // centre of the stencil
+    const float a_c = sqrtf(fmaxf((float)GAMMA * q[C][4] / q[C][0], 0.0f));
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        const float c = q[C][v];
+        float m = 0.0f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) m = fmaxf(m, fabsf(q[s][v] - c));
+        const float eps = (v == 0 || v == 4) ? 1e-4f * fabsf(c) : 1e-4f * a_c;
+        const float inv = 1.0f / (m + eps + 1e-30f);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) put(v * NS + s, (q[s][v] - c) * inv);
+    }
+#pragma unroll
+    for (int k = 5 * NS; k < mlp_kpad(DIM); ++k) put(k, 0.0f);
+}
+
+// ---- tcgen05 helpers ---------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory operand descriptor, K-major, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor: kind::f16, D f32, A and B bf16, both K-major, M x N
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, bool accumulate)
+{
+    const uint32_t acc = accumulate ? 1u : 0u;
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+                 "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar)));
+}
+
+// bounded wait on an mbarrier phase; false after the iteration limit
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long long limit)
+{
+    uint32_t done = 0;
+    for (long long it = 0; it < limit && !done; ++it) {
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity));
+    }
+    return done != 0;
+}
+
+// 16 f32 accumulator columns of this thread's TMEM lane (row)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+struct MlpDev {
+    const __nv_bfloat16 *w1c;   // W1 in the operand layout, 64 rows x KPAD
+    const __nv_bfloat16 *w2c;   // W2 in the operand layout, 64 rows x 64
+    const float *params;        // FP32 parameters (biases, w3, b3 are read from here)
+};
+
+// Fused features + MLP over the cells of a grid (persistent, one 128-cell tile
+// per iteration).  prob (nullable) receives y, flags (nullable) y > threshold.
+// Returns through *err a non-zero code if an MMA completion wait gave up.
+template <int DIM, bool FROM_X>
+__global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const double *U, const __nv_bfloat16 *X,
+                                                           MlpDev w, float threshold, float *prob,
+                                                           unsigned char *flags, int *err)
+{
+    constexpr int KP = mlp_kpad(DIM);
+    extern __shared__ __align__(1024) unsigned char dyn[];
+    __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(dyn);          // 128 x KP
+    __nv_bfloat16 *sW1 = sX + MLP_TILE * KP;                             // 64 x KP
+    __nv_bfloat16 *sH = sW1 + MLP_H * KP;                                // 128 x 64
+    __nv_bfloat16 *sW2 = sH + MLP_TILE * MLP_H;                          // 64 x 64
+    __shared__ __align__(8) uint64_t mbar_mma;
+    __shared__ __align__(8) uint64_t mbar_load;
+    __shared__ uint32_t tmem_base;
+    __shared__ float s_b1[MLP_H], s_b2[MLP_H], s_w3[MLP_H];
+    __shared__ int s_fail;
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar_mma)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar_load)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        s_fail = 0;
+    }
+    if (tid < MLP_H) {
+        s_b1[tid] = w.params[mlp_off_b1(DIM) + tid];
+        s_b2[tid] = w.params[mlp_off_b2(DIM) + tid];
+        s_w3[tid] = w.params[mlp_off_w3(DIM) + tid];
+    }
+    const float b3 = w.params[mlp_off_b3(DIM)];
+    if (tid < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_addr(&tmem_base)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    __syncthreads();
+    // weights: two bulk asynchronous copies completing on mbar_load
+    const uint32_t w1_bytes = MLP_H * KP * 2, w2_bytes = MLP_H * MLP_H * 2;
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&mbar_load)),
+                     "r"(w1_bytes + w2_bytes));
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_addr(sW1)),
+                     "l"(w.w1c), "r"(w1_bytes), "r"(smem_addr(&mbar_load)));
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_addr(sW2)),
+                     "l"(w.w2c), "r"(w2_bytes), "r"(smem_addr(&mbar_load)));
+    }
+    const bool loaded = __syncthreads_and(mbar_wait(&mbar_load, 0, 1ll << 22));
+    if (!loaded && tid == 0) { atomicExch(err, 2); s_fail = 1; }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    __syncthreads();
+    const uint32_t tmem = tmem_base;
+    const int warp = tid >> 5, lane = tid & 31;
+    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
+    const uint32_t idesc = umma_idesc(MLP_TILE, MLP_H);
+    const long long ntiles = (gp.plane + MLP_TILE - 1) / MLP_TILE;
+    uint32_t phase = 0;
+
+    for (long long tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
+        const long long g = tile * MLP_TILE + tid;
+        // features of this thread's cell -> BF16 operand rows
+        if (g < gp.plane && FROM_X) {
+            for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = X[g * KP + k];
+        } else if (g < gp.plane) {
+            cell_features<DIM>(U, gp, g, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
+        } else {
+            for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(0.0f);
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // layer 1: TMEM columns [0, 64)
+        if (tid == 0) {
+            for (int kk = 0; kk < KP / 16; ++kk) {
+                const uint64_t da = umma_desc(smem_addr(sX) + kk * 2 * (MLP_TILE / 8) * 128, (MLP_TILE / 8) * 128, 128);
+                const uint64_t db = umma_desc(smem_addr(sW1) + kk * 2 * (MLP_H / 8) * 128, (MLP_H / 8) * 128, 128);
+                umma_bf16(tmem, da, db, idesc, kk > 0);
+            }
+            umma_commit(&mbar_mma);
+        }
+        bool ok = mbar_wait(&mbar_mma, phase, 1ll << 22);
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (!__syncthreads_and(ok)) { if (tid == 0) { atomicExch(err, 1); s_fail = 1; } break; }
+        // h1 = GELU(z1 + b1) -> BF16 operand of layer 2
+#pragma unroll
+        for (int c0 = 0; c0 < MLP_H; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sH[core_offset(tid, c0 + j, MLP_TILE)] = __float2bfloat16(gelu(v[j] + s_b1[c0 + j]));
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // layer 2: TMEM columns [64, 128)
+        if (tid == 0) {
+            for (int kk = 0; kk < MLP_H / 16; ++kk) {
+                const uint64_t da = umma_desc(smem_addr(sH) + kk * 2 * (MLP_TILE / 8) * 128, (MLP_TILE / 8) * 128, 128);
+                const uint64_t db = umma_desc(smem_addr(sW2) + kk * 2 * (MLP_H / 8) * 128, (MLP_H / 8) * 128, 128);
+                umma_bf16(tmem + MLP_H, da, db, idesc, kk > 0);
+            }
+            umma_commit(&mbar_mma);
+        }
+        ok = mbar_wait(&mbar_mma, phase, 1ll << 22);
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (!__syncthreads_and(ok)) { if (tid == 0) { atomicExch(err, 1); s_fail = 1; } break; }
+        float zz = b3;
+#pragma unroll
+        for (int c0 = 0; c0 < MLP_H; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)(MLP_H + c0), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) zz = fmaf(gelu(v[j] + s_b2[c0 + j]), s_w3[c0 + j], zz);
+        }
+        if (g < gp.plane) {
+            const float y = sigmoidf(zz);
+            if (prob) prob[g] = y;
+            if (flags) flags[g] = (y > threshold) ? 1 : 0;
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
+template <int DIM>
+constexpr int mlp_infer_smem()
+{
+    return (MLP_TILE * mlp_kpad(DIM) + MLP_H * mlp_kpad(DIM) + MLP_TILE * MLP_H + MLP_H * MLP_H) * 2;
+}
+
+} // namespace mmf

@@ -12,7 +12,8 @@
 //                       face state U +- sigma/2 has rho <= 0 or p <= 0 the cell
 //                       falls back to order 1.  A per-cell flag (limit / central)
 //                       selects the limiter; the kernel reports where the limiter
-//                       changed a slope (the troubled-cell labels).
+//                       changed a slope by more than 1e-6 (|rho| + |rho E|) of
+//                       the cell, or fell back (the troubled-cell labels).
 //   stage2d_o2_kernel / stage3d_o2_kernel
 //                       computeRHS with face states U +- sigma/2: every cell
 //                       evaluates a record per face side; border faces use the
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
                 double sl = central;
                 if (limit) {
                     sl = mc_slope<A>(a, b, central);
-                    if (sl != central) act = true;
+                    if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
                 }
                 sig[d][k] = sl;
             }

@@ -239,13 +239,14 @@ def vortex(dim=2, n=64, axis="z", steps=100, cfl=0.5, beta=5.0, periodic=True):
                 cfl, max_steps=steps, periodic=periodic, prm=prm)
 
 
-def radial_sod_ratios(n, p_ratio, rho_ratio, cfl=0.5, max_steps=-1):
+def radial_sod_ratios(n, p_ratio, rho_ratio, cfl=0.5, max_steps=-1, dim=2):
     """[-1,1]^2 radial Sod, r < 0.5: rho = p = 1 inside, p = 1/p_ratio and
     rho = 1/rho_ratio outside, transmissive borders."""
     prm = Params(sod_radius=0.5, sod_rho_in=1.0, sod_p_in=1.0, sod_rho_out=1.0 / rho_ratio,
                  sod_p_out=1.0 / p_ratio)
-    return Case("sod_p%.3g_r%.3g_%d" % (p_ratio, rho_ratio, n), RADSOD, 2, (n, n, 1), (-1.0, -1.0, 0.0), 2.0, cfl,
-                max_steps=max_steps, prm=prm, border_bc=BC_FREE_FLOW)
+    return Case("sod_p%.3g_r%.3g_%d" % (p_ratio, rho_ratio, n), RADSOD, dim, (n, n, n if dim == 3 else 1),
+                (-1.0, -1.0, -1.0 if dim == 3 else 0.0), 2.0, cfl, max_steps=max_steps, prm=prm,
+                border_bc=BC_FREE_FLOW)
 
 
 def batched_sweep(ncases=512, seed=20261203, side_min=32, side_max=512, steps=-1):

@@ -457,7 +457,9 @@ void orc_compute_polynomials(const orc_mesh *m, int problem, int order, const do
                         double mag = fmin(lim, fabs(central));
                         s = (a > 0.0) ? mag : -mag;
                     }
-                    if (s != central) act = 1;
+                    /* activation counts where the slope change is significant
+                     * (round-off level sign flips in flat regions do not) */
+                    if (fabs(s - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[4]))) act = 1;
                 }
                 sd[k] = s;
             }

@@ -1,0 +1,193 @@
+"""The learned troubled-cell indicator on the GPU: training gradients against
+the CPU oracle of the MLP, tcgen05 inference against the oracle forward pass,
+fused (features + MLP) against unfused, features against a numpy restatement,
+and what the trained network buys: order-2 runs where cells predicted smooth
+skip the limiter keep the L1 error of the fully limited run."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def mlp_oracle():
+    import oracle.mlp_oracle as mo
+    return mo
+
+
+def rand_features(n, width, real, seed):
+    import torch
+    from oracle.mlp_oracle import bf16
+    rng = np.random.default_rng(seed)
+    X = np.zeros((n, width), dtype=np.float64)
+    X[:, :real] = bf16(rng.uniform(-1, 1, (n, real)))
+    bits = (X.astype(np.float32).view(np.uint32) >> 16).astype(np.uint16).view(np.int16)
+    return X, torch.from_numpy(bits.copy()).cuda()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gradients_match_cpu_oracle(mmf, dim):
+    import torch
+    from minimmerflow_gb300.indicator import TroubledCellMLP
+    mo = mlp_oracle()
+    mlp = TroubledCellMLP(dim=dim, seed=5)
+    real = 135 if dim == 3 else 45
+    X, dX = rand_features(256, mlp.width, real, 1)
+    y = (np.random.default_rng(2).random(256) < 0.3).astype(np.uint8)
+    dy = torch.from_numpy(y).cuda()
+    # non-zero biases so that every term is exercised
+    p = mlp.params()
+    p[mo.H * mlp.width:] += np.random.default_rng(3).normal(0, 0.1, p.size - mo.H * mlp.width).astype(np.float32)
+    mlp.set_params(p)
+    g, loss = mlp.gradients(dX, dy, 256)
+    loss_ref, g_ref = mo.loss_and_grad(p.astype(np.float64), X, y, mlp.width)
+    assert abs(loss - loss_ref) <= 1e-5 * max(1.0, abs(loss_ref))
+    rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert rel < 2e-4, rel
+    # every block individually
+    off = [0, mo.H * mlp.width, mo.H * mlp.width + mo.H, mo.H * mlp.width + mo.H + mo.H * mo.H]
+    for a, b in zip(off, off[1:] + [g.size]):
+        assert np.linalg.norm(g[a:b] - g_ref[a:b]) <= 1e-3 * np.linalg.norm(g_ref[a:b]) + 1e-9
+
+
+@pytest.mark.parametrize("dim,n", [(3, 1000), (2, 777), (3, 128)])
+def test_tcgen05_predict_matches_oracle(mmf, dim, n):
+    import torch
+    from minimmerflow_gb300.indicator import TroubledCellMLP
+    mo = mlp_oracle()
+    mlp = TroubledCellMLP(dim=dim, seed=11)
+    real = 135 if dim == 3 else 45
+    X, dX = rand_features(n, mlp.width, real, 4)
+    p = mlp.params()
+    p[mo.H * mlp.width:] += np.random.default_rng(6).normal(0, 0.2, p.size - mo.H * mlp.width).astype(np.float32)
+    mlp.set_params(p)
+    prob = torch.empty(n, dtype=torch.float32, device="cuda")
+    mlp.predict(dX, prob)
+    ref, _ = mo.forward(p.astype(np.float64), X, mlp.width)
+    assert np.abs(prob.cpu().numpy() - ref).max() < 2e-4
+
+
+def numpy_features(U, dim, n, periodic):
+    """Features of every cell (x fastest), FP64 restatement of the kernel's definition."""
+    g = 1.4
+    rho = U[:, 0]
+    u, v, w = U[:, 1] / rho, U[:, 2] / rho, U[:, 3] / rho
+    p = (g - 1) * (U[:, 4] - 0.5 * rho * (u * u + v * v + w * w))
+    shape = (n[2], n[1], n[0]) if dim == 3 else (n[1], n[0])
+    q = [a.reshape(shape) for a in (rho, u, v, w, p)]
+    offs = [(dz, dy, dx) for dz in ((-1, 0, 1) if dim == 3 else (0,)) for dy in (-1, 0, 1) for dx in (-1, 0, 1)]
+    mode = "wrap" if periodic else "edge"
+    out = []
+    a_c = np.sqrt(np.maximum(g * q[4] / q[0], 0))
+    for vi in range(5):
+        pad = np.pad(q[vi], 1, mode=mode)
+        st = []
+        for dz, dy, dx in offs:
+            if dim == 3:
+                st.append(pad[1 + dz:1 + dz + shape[0], 1 + dy:1 + dy + shape[1], 1 + dx:1 + dx + shape[2]])
+            else:
+                st.append(pad[1 + dy:1 + dy + shape[0], 1 + dx:1 + dx + shape[1]])
+        st = np.stack(st)
+        c = q[vi]
+        m = np.abs(st - c).max(axis=0)
+        eps = 1e-4 * np.abs(c) if vi in (0, 4) else 1e-4 * a_c
+        out.append(((st - c) / (m + eps + 1e-30)).reshape(len(offs), -1).T)
+    return np.concatenate(out, axis=1)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_features_match_numpy(mmf, dim):
+    import torch
+    from minimmerflow_gb300 import indicator
+    from oracle.mlp_oracle import bf16_bits_to_float
+    case = mmf.problem.vortex(dim, 12, steps=1) if dim == 3 else mmf.problem.radial_sod_2d(n=20)
+    U = case.initial_state()
+    with case.solver(arith="fast", order=2) as s:
+        s.upload(U)
+        X = indicator.features(s).cpu().numpy()
+    F = bf16_bits_to_float(X.view(np.uint16))
+    ref = numpy_features(U, dim, case.n, case.periodic)
+    real = ref.shape[1]
+    assert np.abs(F[:, :real] - ref).max() < 1e-2
+    assert np.all(F[:, real:] == 0)
+
+
+def train_small(mmf, dim, seed=0):
+    """A quickly trained indicator from seeded Sod and vortex order-2 runs."""
+    from minimmerflow_gb300 import indicator
+    P = mmf.problem
+    if dim == 2:
+        cases = [P.radial_sod_ratios(64, 8.0, 4.0), P.radial_sod_ratios(48, 40.0, 8.0),
+                 P.vortex(2, 64, beta=5.0), P.vortex(2, 48, beta=2.0)]
+    else:
+        cases = [P.radial_sod_ratios(24, 10.0, 8.0, dim=3), P.vortex(3, 24, beta=5.0)]
+    X, y = indicator.generate_dataset(cases, snapshots=4, steps_between=5, samples=0, seed=seed)
+    mlp = indicator.TroubledCellMLP(dim=dim, seed=seed)
+    losses = mlp.fit(X, y, epochs=30, batch=512, lr=3e-3, seed=seed)
+    return mlp, X, y, losses
+
+
+def test_training_learns_the_limiter(mmf):
+    import torch
+    mlp, X, y, losses = train_small(mmf, 2)
+    assert losses[-1] < 0.6 * losses[0]
+    prob = torch.empty(X.shape[0], dtype=torch.float32, device="cuda")
+    mlp.predict(X, prob)
+    pr = prob.cpu().numpy()
+    yy = y.cpu().numpy().astype(bool)
+    recall = (pr[yy] > 0.1).mean()
+    skipped = (pr < 0.1).mean()
+    assert recall > 0.9, recall
+    assert skipped > 0.3, skipped
+
+
+def test_fused_indicator_equals_features_then_predict(mmf):
+    import torch
+    from minimmerflow_gb300 import indicator
+    mlp = indicator.TroubledCellMLP(dim=3, seed=7)
+    case = mmf.problem.vortex(3, 16, steps=1)
+    with case.solver(arith="fast", order=2) as s:
+        s.upload(case.initial_state())
+        X = indicator.features(s)
+        p_fused, f_fused = indicator.run_indicator(s, mlp, 0.5)
+    prob = torch.empty(X.shape[0], dtype=torch.float32, device="cuda")
+    mlp.predict(X, prob)
+    p = prob.cpu().numpy()
+    assert np.abs(p - p_fused).max() < 1e-3
+    assert np.mean(p == p_fused) > 0.99
+    assert np.array_equal(f_fused, (p_fused > 0.5).astype(np.uint8))
+
+
+def test_learned_limiter_keeps_vortex_accuracy(orc, mmf):
+    """2D vortex 64^2, periodic, order 2, 100 steps: the run whose smooth cells
+    (per the trained indicator) skip the limiter has an L1 density error no
+    more than 1% above the fully limited run (it is in fact lower: central
+    slopes at smooth extrema are more accurate than clipped ones)."""
+    from minimmerflow_gb300 import indicator
+    mlp, _, _, _ = train_small(mmf, 2, seed=1)
+    case = mmf.problem.vortex(2, 64, steps=100)
+    U0 = case.initial_state()
+    with case.solver(arith="fast", order=2) as s:
+        U_plain, t, _ = s.run(U0, case.cfl, max_steps=100)
+    with case.solver(arith="fast", order=2) as s:
+        indicator.use_indicator(s, mlp, 0.1)
+        U_learn, t2, _ = s.run(U0, case.cfl, max_steps=100)
+        assert s.status() == 0
+    e_plain = case.l1_density_error(U_plain, t)
+    e_learn = case.l1_density_error(U_learn, t2)
+    assert e_learn <= 1.01 * e_plain, (e_learn, e_plain)
+
+
+def test_learned_limiter_on_sod_stays_physical(mmf):
+    """3D radial Sod with the learned limiter: no negative pressure or NaN, and
+    the state stays close to the fully limited run."""
+    from minimmerflow_gb300 import indicator
+    mlp, _, _, _ = train_small(mmf, 3, seed=2)
+    case = mmf.problem.radial_sod_ratios(24, 10.0, 8.0, dim=3)
+    U0 = case.initial_state()
+    with case.solver(arith="fast", order=2) as s:
+        U_plain, _, _ = s.run(U0, case.cfl, max_steps=20)
+    with case.solver(arith="fast", order=2) as s:
+        indicator.use_indicator(s, mlp, 0.1)
+        U_learn, _, _ = s.run(U0, case.cfl, max_steps=20)
+        assert s.status() == 0
+    assert np.abs(U_learn - U_plain).sum() < 2e-3 * np.abs(U_plain).sum()
