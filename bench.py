@@ -21,6 +21,8 @@ cpu_baseline: the oracle (C restatement, bit-identical to the reference
 """
 import argparse
 import json
+
+import numpy as np
 import math
 import os
 import statistics
@@ -238,6 +240,65 @@ def run_batched(args, world, rank, local, dist):
                 plain=plain_value, status_bad=status_bad, ncases=len(cases))
 
 
+def run_learned(args, world, rank, local, dist):
+    """3D radial Sod (order 2, MC limiter) with and without the learned
+    troubled-cell indicator; accuracy against the exact solution on a 3D
+    isentropic vortex with the same two settings."""
+    import torch
+    import minimmerflow_gb300 as mmf
+    from minimmerflow_gb300 import indicator, train_indicator
+
+    torch.cuda.set_device(local)
+    mlp = train_indicator.load(3, device=local)
+    trained_here = mlp is None
+    if mlp is None:
+        mlp, _, _ = train_indicator.train(3, samples=1_000_000, epochs=8, log=None)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    case = mmf.problem.radial_sod_ratios(args.n, 10.0, 8.0, dim=3)
+    U0 = case.initial_state()
+    out = {}
+    finals = {}
+    for mode in ("plain", "learned"):
+        s = case.solver(arith=args.arith, device=local, order=2)
+        if mode == "learned":
+            indicator.use_indicator(s, mlp, args.threshold)
+        stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
+        s.advance(args.warmup)
+        launches0 = s.launch_count
+        durs = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.advance_async(1)
+            e1.record(stream)
+            e1.synchronize()
+            durs.append(e0.elapsed_time(e1) / 1e3)
+        out[mode] = dict(value=case.ncells * args.steps / sum(durs), ms=1e3 * sum(durs) / args.steps,
+                         launches=s.launch_count - launches0, status=s.status())
+        finals[mode] = s.download()
+        if mode == "learned":
+            _, flags = indicator.run_indicator(s, mlp, args.threshold)
+            out[mode]["limited_fraction"] = float(flags.mean())
+        s.close()
+    diff = float(np.abs(finals["learned"][:, 0] - finals["plain"][:, 0]).sum() / np.abs(finals["plain"][:, 0]).sum())
+    # accuracy against the exact vortex (3D, periodic, 50 steps)
+    vc = mmf.problem.vortex(3, args.vortex_n, steps=50)
+    V0 = vc.initial_state()
+    errs = {}
+    for mode in ("plain", "learned"):
+        with vc.solver(arith=args.arith, device=local, order=2) as s:
+            if mode == "learned":
+                indicator.use_indicator(s, mlp, args.threshold)
+            V, t, _ = s.run(V0, vc.cfl, max_steps=50)
+        errs[mode] = vc.l1_density_error(V, t)
+    return dict(out=out, diff=diff, errs=errs, ncell=case.ncells, trained_here=trained_here)
+
+
 def make_case(args):
     import minimmerflow_gb300 as mmf
     if args.workload == "sod2d":
@@ -249,6 +310,12 @@ def make_case(args):
 
 
 def workload_config(args, world):
+    if args.workload == "sod3d_learned":
+        return {"workload": ("3D radial Sod %d^3, [-1,1]^3, r<0.5, p-ratio 10, rho-ratio 8, transmissive, CFL 0.5, "
+                             "order 2 MC-limited, learned troubled-cell indicator (135-64-64-1, BF16 tcgen05) "
+                             "gating the limiter at threshold %.2f, FP64 state" % (args.n, args.threshold)),
+                "cells": args.n ** 3, "l2": "flushed between timed steps (512 MB write)",
+                "parallelism": "replicas x%d" % world}
     if args.workload == "batched":
         return {"workload": ("batched sweep: %d independent 2D cases (seed %d), side U{32..512}, half isentropic "
                              "vortices beta~U[1,8] (periodic [-5,5]^2), half radial Sods p-ratio logU[2,100], "
@@ -377,7 +444,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
-    ap.add_argument("--workload", default="sod2d", choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched"])
+    ap.add_argument("--workload", default="sod2d",
+                    choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned"])
+    ap.add_argument("--threshold", type=float, default=0.1)
+    ap.add_argument("--vortex-n", type=int, default=64)
     ap.add_argument("--ncases", type=int, default=512)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=0)
@@ -409,6 +479,26 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.workload == "sod3d_learned":
+        r = run_learned(args, world, rank, local, dist)
+        if rank != 0:
+            return
+        o = r["out"]
+        line = {"metric": metric, "value": o["learned"]["value"], "unit": metric, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": o["learned"]["ms"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": workload, "arith": args.arith,
+                "plain_order2": {"value": o["plain"]["value"], "ms_per_step": o["plain"]["ms"]},
+                "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
+                "limited_fraction_final_state": o["learned"]["limited_fraction"],
+                "sod_l1_density_difference_learned_vs_plain": r["diff"],
+                "vortex3d_l1_error": {"plain": r["errs"]["plain"], "learned": r["errs"]["learned"],
+                                      "ratio": r["errs"]["learned"] / r["errs"]["plain"],
+                                      "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2" % args.vortex_n},
+                "indicator_trained_in_this_run": r["trained_here"],
+                "gpu_launches": o["learned"]["launches"]}
+        print(json.dumps(line))
+        return
     if args.workload == "batched":
         r = run_batched(args, world, rank, local, dist)
         if rank != 0:
