@@ -181,8 +181,21 @@ def run_batched(args, world, rank, local, dist):
 
     torch.cuda.set_device(local)
     cases = mmf.problem.batched_sweep(ncases=args.ncases, seed=args.seed)
+    if args.order == 2:
+        for c in cases:
+            c.cfl = args.cfl_order2
     states = [c.initial_state() for c in cases]
-    b = BatchEuler(cases, arith=args.arith, device=local)
+    b = BatchEuler(cases, arith=args.arith, device=local, order=args.order)
+    mlp = None
+    if args.learned:
+        from minimmerflow_gb300 import train_indicator
+        mlp, thr = train_indicator.load(2, device=local)
+        if mlp is None:
+            mlp, _, thr = train_indicator.train(2, samples=1_000_000, epochs=8, log=None)
+        if args.threshold > 0:
+            thr = args.threshold
+        args.threshold = thr
+        b.set_indicator(mlp, thr)
     b.upload(states)
     horizon = args.warmup + args.steps + 64
     b.time_setup(max_steps=horizon)
@@ -217,12 +230,17 @@ def run_batched(args, world, rank, local, dist):
         total = float(tt.item())
     value = world * b.total * args.steps / total
     status_bad = sum(1 for i in range(len(cases)) if b.case_info(i)[2])
+    # accuracy: the vortex cases after 'acc_steps' steps against the exact solution
+    acc = None
+    if args.order == 2:
+        acc_steps = 20
+        out_b = b.run(states, acc_steps)
     b.close()
-    # plain: single-case contexts one after another
+    # plain: single-case contexts one after another (order-2 plain = limiter on every cell)
     k_plain = max(2, min(args.steps, 8))
     ctxs = []
     for c, U0 in zip(cases, states):
-        s = c.solver(arith=args.arith, device=local)
+        s = c.solver(arith=args.arith, device=local, order=args.order)
         s.upload(U0)
         s.time_setup(c.cfl, 0.0, math.inf, 10 ** 9)
         s.advance(1)
@@ -230,14 +248,32 @@ def run_batched(args, world, rank, local, dist):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in ctxs:
-        s.advance(k_plain)
+        try:
+            s.advance(k_plain)
+        except mmf.capi.MMFError:
+            pass
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     plain_value = sum(c.ncells for c in cases) * k_plain / plain_s
+    if args.order == 2:
+        ratios = []
+        for i, (c, s, U0) in enumerate(zip(cases, ctxs, states)):
+            if c.problem != mmf.problem.VORTEX_XY:
+                continue
+            try:
+                Up, tp, _ = s.run(U0, c.cfl, max_steps=acc_steps)
+            except mmf.capi.MMFError:
+                continue
+            ep = c.l1_density_error(Up, tp)
+            el = c.l1_density_error(out_b[i], tp)
+            ratios.append(el / ep)
+        acc = {"vortex_cases": len(ratios), "steps": acc_steps,
+               "l1_error_ratio_batched_learned_over_plain": {"mean": float(np.mean(ratios)),
+                                                             "max": float(np.max(ratios))}}
     for s in ctxs:
         s.close()
     return dict(value=value, total=total, clocks=clocks, launches=launches, ncell=b.total, chunk=chunk, bps=bps,
-                plain=plain_value, status_bad=status_bad, ncases=len(cases))
+                plain=plain_value, status_bad=status_bad, ncases=len(cases), accuracy=acc)
 
 
 def run_learned(args, world, rank, local, dist):
@@ -249,10 +285,13 @@ def run_learned(args, world, rank, local, dist):
     from minimmerflow_gb300 import indicator, train_indicator
 
     torch.cuda.set_device(local)
-    mlp = train_indicator.load(3, device=local)
+    mlp, thr = train_indicator.load(3, device=local)
     trained_here = mlp is None
     if mlp is None:
-        mlp, _, _ = train_indicator.train(3, samples=1_000_000, epochs=8, log=None)
+        mlp, _, thr = train_indicator.train(3, samples=1_000_000, epochs=8, log=None)
+    if args.threshold > 0:
+        thr = args.threshold
+    args.threshold = thr
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     case = mmf.problem.radial_sod_ratios(args.n, 10.0, 8.0, dim=3)
     U0 = case.initial_state()
@@ -310,10 +349,17 @@ def make_case(args):
 
 
 def workload_config(args, world):
+    if args.workload == "batched" and args.order == 2:
+        return {"workload": ("batched sweep, order 2 MC-limited%s: %d independent 2D cases (seed %d), side U{32..512}, "
+                             "half isentropic vortices beta~U[1,8] (periodic [-5,5]^2), half radial Sods p-ratio "
+                             "logU[2,100], rho-ratio U[2,10] (transmissive [-1,1]^2), CFL %.2f per case, FP64"
+                             % (", learned indicator (45-64-64-1, BF16 tcgen05) at threshold %.4f" % args.threshold
+                                if args.learned else "", args.ncases, args.seed, args.cfl_order2)),
+                "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
     if args.workload == "sod3d_learned":
         return {"workload": ("3D radial Sod %d^3, [-1,1]^3, r<0.5, p-ratio 10, rho-ratio 8, transmissive, CFL 0.5, "
                              "order 2 MC-limited, learned troubled-cell indicator (135-64-64-1, BF16 tcgen05) "
-                             "gating the limiter at threshold %.2f, FP64 state" % (args.n, args.threshold)),
+                             "gating the limiter at threshold %.4f, FP64 state" % (args.n, args.threshold)),
                 "cells": args.n ** 3, "l2": "flushed between timed steps (512 MB write)",
                 "parallelism": "replicas x%d" % world}
     if args.workload == "batched":
@@ -446,7 +492,9 @@ def main():
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
     ap.add_argument("--workload", default="sod2d",
                     choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned"])
-    ap.add_argument("--threshold", type=float, default=0.1)
+    ap.add_argument("--threshold", type=float, default=0.0, help="0 = the calibrated threshold of the weights file")
+    ap.add_argument("--learned", action="store_true")
+    ap.add_argument("--cfl-order2", type=float, default=0.4)
     ap.add_argument("--vortex-n", type=int, default=64)
     ap.add_argument("--ncases", type=int, default=512)
     ap.add_argument("--seed", type=int, default=20261203)
@@ -487,7 +535,7 @@ def main():
         line = {"metric": metric, "value": o["learned"]["value"], "unit": metric, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": o["learned"]["ms"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": workload, "arith": args.arith,
+                "data": "synthetic", "config": workload_config(args, world), "arith": args.arith,
                 "plain_order2": {"value": o["plain"]["value"], "ms_per_step": o["plain"]["ms"]},
                 "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
                 "limited_fraction_final_state": o["learned"]["limited_fraction"],
@@ -507,14 +555,18 @@ def main():
         line = {"metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(workload, cells=r["ncell"], autotuned_chunk=r["chunk"], blocks_per_sm=r["bps"]),
+                "config": dict(workload_config(args, world), cells=r["ncell"], autotuned_chunk=r["chunk"],
+                               blocks_per_sm=r["bps"]),
                 "arith": args.arith,
                 "roofline": {"bound": "hbm", "kernel": "stage2d_batch_kernel (3 per step)",
                              "achieved": CELL_BYTES_STEP * r["value"] / world / 1e9, "peak": hbm_peak, "unit": "GB/s",
                              "frac": CELL_BYTES_STEP * r["value"] / world / 1e9 / hbm_peak, "peak_source": peak_src,
                              "traffic": None},
                 "plain_single_case_contexts": {"value": r["plain"], "unit": metric,
-                                               "how": "same cases, one context each, run one after another"},
+                                               "how": "same cases, one context each, run one after another"
+                                                      + (", limiter on every cell" if args.order == 2 else "")},
+                "over_plain": r["value"] / r["plain"],
+                "accuracy": r["accuracy"],
                 "clocks": r["clocks"], "gpu_launches": r["launches"], "cases_with_status": r["status_bad"]}
         print(json.dumps(line))
         return

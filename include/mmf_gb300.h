@@ -158,12 +158,13 @@ int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const doubl
                        const double *dirichlet_prim, double *cons_bc);
 
 /* ---- batched cases ------------------------------------------------------ */
-/* Many independent 2D order-1 cases of uneven size advanced together: one
+/* Many independent 2D cases of uneven size advanced together: one
  * persistent launch per RK stage walks a list of (case, segment, row chunk)
  * work items, each case keeps its own t, CFL dt (per-case maxEig reduction),
  * step count and status, and the step sequence replays from a CUDA graph.
  * Each case gets exactly the result of its own single-case context.  No
- * reference counterpart (the reference runs one case per process). */
+ * reference counterpart (the reference runs one case per process).  Order 1
+ * or order 2 (all cases alike). */
 typedef struct mmf_batch mmf_batch;
 int mmf_batch_create(int ncases, const mmf_grid *grids, int device, mmf_batch **out);
 int mmf_batch_destroy(mmf_batch *batch);
@@ -178,6 +179,11 @@ int mmf_batch_time_setup(mmf_batch *batch, const double *cfl, const double *t_en
 int mmf_batch_advance_async(mmf_batch *batch, int64_t n_steps);
 int mmf_batch_synchronize(mmf_batch *batch);
 int mmf_batch_case_info(mmf_batch *batch, int c, double *t, int64_t *steps, unsigned *status);
+/* Order-2 batches: limiter mode for every case (MMF_LIMIT_*), and the learned
+ * indicator (a 2D mmf_mlp) run at the start of every step over all cases. */
+typedef struct mmf_mlp mmf_mlp;
+int mmf_batch_set_limiter(mmf_batch *batch, int mode);
+int mmf_batch_set_indicator(mmf_batch *batch, mmf_mlp *mlp, float threshold);
 /* Decomposition: rows per work item and resident blocks per SM (0 = occupancy maximum). */
 int mmf_batch_set_shape(mmf_batch *batch, int chunk, int blocks_per_sm);
 int mmf_batch_get_shape(mmf_batch *batch, int *chunk, int *blocks_per_sm);

@@ -12,7 +12,7 @@ from .solver import _bc
 class BatchEuler:
     """Context over a list of 2D problem cases (minimmerflow_gb300.problem.Case)."""
 
-    def __init__(self, cases, arith="fast", device=0):
+    def __init__(self, cases, arith="fast", device=0, order=1):
         self._lib = capi.load()
         self.cases = list(cases)
         grids = (capi.Grid * len(self.cases))()
@@ -27,7 +27,7 @@ class BatchEuler:
                 g.bc_lo[d] = _bc(lo[d]) if d < 2 else 0
                 g.bc_hi[d] = _bc(hi[d]) if d < 2 else 0
             g.h = case.h
-            g.order = 1
+            g.order = order
             g.arith = {"reference": capi.ARITH_REFERENCE, "fast": capi.ARITH_FAST}[arith]
         self._b = C.c_void_p()
         capi.check(self._lib.mmf_batch_create(len(self.cases), grids, device, C.byref(self._b)))
@@ -95,6 +95,14 @@ class BatchEuler:
         a, b = C.c_int(), C.c_int()
         capi.check(self._lib.mmf_batch_autotune(self._b, trial_steps, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_limiter(self, mode):
+        m = {"all": capi.LIMIT_ALL, "none": capi.LIMIT_NONE, "flagged": capi.LIMIT_FLAGGED}.get(mode, mode)
+        capi.check(self._lib.mmf_batch_set_limiter(self._b, m))
+
+    def set_indicator(self, mlp, threshold):
+        """Order-2 batches: the learned indicator (2D) gates the limiter of every case."""
+        capi.check(self._lib.mmf_batch_set_indicator(self._b, mlp.handle if mlp is not None else None, threshold))
 
     @property
     def stream_handle(self):

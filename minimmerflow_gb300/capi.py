@@ -25,7 +25,7 @@ EXPORTS = [
     "mmf_batch_create", "mmf_batch_destroy", "mmf_batch_cell_count", "mmf_batch_launch_count",
     "mmf_batch_get_stream", "mmf_batch_upload", "mmf_batch_download", "mmf_batch_time_setup",
     "mmf_batch_advance_async", "mmf_batch_synchronize", "mmf_batch_case_info", "mmf_batch_set_shape",
-    "mmf_batch_get_shape", "mmf_batch_autotune",
+    "mmf_batch_get_shape", "mmf_batch_autotune", "mmf_batch_set_limiter", "mmf_batch_set_indicator",
     "mmf_mlp_create", "mmf_mlp_destroy", "mmf_mlp_num_params", "mmf_mlp_input_width", "mmf_mlp_get_params",
     "mmf_mlp_set_params", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
     "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
@@ -107,6 +107,8 @@ def load(build_if_missing=True):
     L.mmf_batch_case_info.argtypes = [_P, C.c_int, _D, C.POINTER(C.c_int64), C.POINTER(C.c_uint)]
     L.mmf_batch_set_shape.argtypes = [_P, C.c_int, C.c_int]
     L.mmf_batch_get_shape.argtypes = [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mmf_batch_set_limiter.argtypes = [_P, C.c_int]
+    L.mmf_batch_set_indicator.argtypes = [_P, _P, C.c_float]
     L.mmf_batch_autotune.argtypes = [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.mmf_mlp_create.argtypes = [C.c_int, C.c_uint64, C.c_int, C.POINTER(_P)]
     L.mmf_mlp_destroy.argtypes = [_P]

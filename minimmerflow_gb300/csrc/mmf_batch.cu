@@ -18,6 +18,9 @@
 
 namespace mmf {
 int set_last_error(int code, const char *msg);
+cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
+                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s);
+int mlp_dim(const mmf_mlp *p);
 }
 using namespace mmf;
 
@@ -83,6 +86,14 @@ struct mmf_batch {
     cudaGraphExec_t g_many = nullptr, g_one = nullptr;
     long long launches = 0;
     bool time_ready = false;
+    // order 2
+    int order = 1;
+    double *S = nullptr;
+    unsigned char *lim_flag = nullptr, *lim_active = nullptr;
+    int limit_mode = LIMIT_ALL;
+    long long *d_offsets = nullptr;
+    mmf_mlp *indicator = nullptr;
+    float ind_threshold = 0.5f;
 
     void drop_graphs()
     {
@@ -99,13 +110,41 @@ struct mmf_batch {
                    ? launch_batch_fast(st, cases, item_case, nitems, ctrl, base, blocks, stream, w_zero)
                    : launch_batch_exact(st, cases, item_case, nitems, ctrl, base, blocks, stream);
     }
+    cudaError_t o2(int op, int st, const double *state, double *out)
+    {
+        StageArgs base;
+        base.U = U; base.R = R; base.W = W; base.out = out; base.ctrl = nullptr; base.rhs_maxeig = nullptr;
+        O2Batch ob;
+        ob.S = S; ob.flag = lim_flag; ob.active = (op == BO2_SLOPES && st == STAGE_1) ? lim_active : nullptr;
+        ob.limit_mode = limit_mode;
+        ++launches;
+        return arith == MMF_ARITH_FAST
+                   ? launch_batch_o2_fast(op, st, cases, item_case, nitems, ctrl, base, state, ob, W, blocks, stream, w_zero)
+                   : launch_batch_o2_exact(op, st, cases, item_case, nitems, ctrl, base, state, ob, W, blocks, stream);
+    }
     cudaError_t rk_step()
     {
         cudaError_t e;
+        if (order == 2) {
+            if (indicator) {
+                ++launches;
+                if ((e = mlp_indicator_batch(indicator, cases, d_offsets, ncases, total, U, ind_threshold, lim_flag,
+                                             stream)) != cudaSuccess)
+                    return e;
+            }
+            if ((e = o2(BO2_SLOPES, STAGE_1, U, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(BO2_STAGE, STAGE_1, U, R)) != cudaSuccess) return e;
+            if ((e = o2(BO2_FORM_W1, STAGE_2, U, W)) != cudaSuccess) return e;
+            if ((e = o2(BO2_SLOPES, STAGE_2, W, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(BO2_STAGE, STAGE_2, W, R)) != cudaSuccess) return e;
+            if ((e = o2(BO2_SLOPES, STAGE_3, R, nullptr)) != cudaSuccess) return e;
+            return o2(BO2_STAGE, STAGE_3, R, U);
+        }
         if ((e = stage(STAGE_1, R)) != cudaSuccess) return e;
         if ((e = stage(STAGE_2, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U);
     }
+    int launches_per_step() const { return order == 2 ? (indicator ? 8 : 7) : 3; }
 };
 
 static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
@@ -184,12 +223,12 @@ static int batch_enqueue(mmf_batch *b, int64_t n_steps)
     int64_t left = n_steps;
     while (left >= GRAPH_STEPS) {
         BATCH_CUDA(cudaGraphLaunch(b->g_many, b->stream));
-        b->launches += 3 * GRAPH_STEPS;
+        b->launches += b->launches_per_step() * GRAPH_STEPS;
         left -= GRAPH_STEPS;
     }
     while (left-- > 0) {
         BATCH_CUDA(cudaGraphLaunch(b->g_one, b->stream));
-        b->launches += 3;
+        b->launches += b->launches_per_step();
     }
     return MMF_OK;
 }
@@ -206,7 +245,8 @@ int mmf_batch_create(int ncases, const mmf_grid *grids, int device, mmf_batch **
     for (int c = 0; c < ncases; ++c) {
         const mmf_grid &g = grids[c];
         if (g.dim != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "batched cases are 2D");
-        if (g.order != 1) return set_last_error(MMF_ERR_UNSUPPORTED, "batched cases use order 1");
+        if (g.order != 1 && g.order != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "order must be 1 or 2");
+        if (g.order != grids[0].order) return set_last_error(MMF_ERR_ARG, "all cases need the same order");
         if (g.arith != arith) return set_last_error(MMF_ERR_ARG, "all cases need the same arithmetic");
         if (arith != MMF_ARITH_REFERENCE && arith != MMF_ARITH_FAST) return set_last_error(MMF_ERR_ARG, "unknown arithmetic");
         if (!(g.h > 0.0) || g.n[0] < 1 || g.n[1] < 1) return set_last_error(MMF_ERR_ARG, "bad grid");
@@ -227,6 +267,7 @@ int mmf_batch_create(int ncases, const mmf_grid *grids, int device, mmf_batch **
     b->total = total;
     b->grids.assign(grids, grids + ncases);
     b->offsets = offsets;
+    b->order = grids[0].order;
     cudaDeviceProp prop;
     cudaError_t e = cudaGetDeviceProperties(&prop, device);
     b->sms = (e == cudaSuccess) ? prop.multiProcessorCount : 1;
@@ -240,6 +281,19 @@ int mmf_batch_create(int ncases, const mmf_grid *grids, int device, mmf_batch **
     if (e == cudaSuccess) e = cudaMalloc(&b->flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(b->U, 0, bytes, b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl) * ncases, b->stream);
+    if (e == cudaSuccess && b->order == 2) {
+        e = cudaMalloc(&b->S, bytes * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&b->lim_flag, (size_t)total);
+        if (e == cudaSuccess) e = cudaMalloc(&b->lim_active, (size_t)total);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_offsets, sizeof(long long) * (ncases + 1));
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->lim_flag, 0, (size_t)total, b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->lim_active, 0, (size_t)total, b->stream);
+        std::vector<long long> offs(offsets);
+        offs.push_back(total);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->d_offsets, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    }
     if (e != cudaSuccess) {
         std::string msg = cudaGetErrorString(e);
         mmf_batch_destroy(b);
@@ -259,6 +313,7 @@ int mmf_batch_destroy(mmf_batch *b)
     b->drop_graphs();
     cudaFree(b->U); cudaFree(b->R); cudaFree(b->W); cudaFree(b->aos); cudaFree(b->ctrl); cudaFree(b->flag);
     cudaFree(b->cases); cudaFree(b->item_case);
+    cudaFree(b->S); cudaFree(b->lim_flag); cudaFree(b->lim_active); cudaFree(b->d_offsets);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return MMF_OK;
@@ -379,13 +434,38 @@ int mmf_batch_get_shape(mmf_batch *b, int *chunk, int *blocks_per_sm)
     return MMF_OK;
 }
 
+int mmf_batch_set_limiter(mmf_batch *b, int mode)
+{
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (b->order != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "the limiter applies to order 2");
+    if (mode != LIMIT_ALL && mode != LIMIT_NONE && mode != LIMIT_FLAGGED) return set_last_error(MMF_ERR_ARG, "unknown limiter mode");
+    b->limit_mode = mode;
+    b->drop_graphs();
+    return MMF_OK;
+}
+
+int mmf_batch_set_indicator(mmf_batch *b, mmf_mlp *mlp, float threshold)
+{
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (b->order != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
+    if (mlp && mlp_dim(mlp) != 2) return set_last_error(MMF_ERR_ARG, "batched cases need a 2D indicator");
+    b->indicator = mlp;
+    b->ind_threshold = threshold;
+    b->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;
+    b->drop_graphs();
+    return MMF_OK;
+}
+
 int mmf_batch_autotune(mmf_batch *b, int trial_steps, int *chunk_out, int *blocks_per_sm_out)
 {
     int rc = batch_check(b);
     if (rc) return rc;
     if (!b->time_ready) return set_last_error(MMF_ERR_ARG, "mmf_batch_time_setup first");
     if (trial_steps < 1) trial_steps = 4;
-    const auto key = std::make_tuple(b->arith * 2 + (b->w_zero ? 1 : 0), b->total, b->ncases, b->sms);
+    const auto key = std::make_tuple(b->arith * 8 + (b->w_zero ? 1 : 0) + (b->order == 2 ? 2 : 0) + (b->indicator ? 4 : 0),
+                                     b->total, b->ncases, b->sms);
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tuned.find(key);

@@ -14,6 +14,7 @@
 #pragma once
 
 #include "mmf_cartesian.cuh"
+#include "mmf_order2.cuh"
 
 namespace mmf {
 
@@ -75,6 +76,139 @@ inline int batch_blocks_per_sm()
         return 1;
     return nb > 0 ? nb : 1;
 }
+
+// ---- order 2 -----------------------------------------------------------------
+struct O2Batch {
+    double *S;                 // packed slopes: plane (d * NV + k) at S + (d * NV + k) * total
+    unsigned char *flag;       // packed limiter flags
+    unsigned char *active;     // packed limiter activity (nullable)
+    int limit_mode;
+};
+
+// Walks the item list; for each item of an active case calls body(gp, off, ctrl, seg, chunk).
+template <class Body>
+__device__ __forceinline__ void for_items(const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
+                                          Body body)
+{
+    const int warp0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int item = warp0; item < nitems; item += nwarps) {
+        const int c = item_case[item];
+        const GridParams gp = cases[c].gp;
+        const int local = item - cases[c].item0;
+        body(gp, cases[c].offset, cctrl + c, local % gp.nseg, local / gp.nseg, local == 0);
+    }
+}
+
+// slopes (computePolynomials) of the output cells of every item
+template <class A>
+__global__ void __launch_bounds__(128) slopes_batch_kernel(const CaseDesc *__restrict__ cases,
+                                                           const int *__restrict__ item_case, int nitems, Ctrl *cctrl,
+                                                           const double *state, O2Batch ob, int stage)
+{
+    const int lane = threadIdx.x & 31;
+    for_items(cases, item_case, nitems, cctrl, [&](const GridParams &gp, long long off, Ctrl *ctrl, int seg, int chunk,
+                                                   bool) {
+        if (!o2_step_active(ctrl, stage)) return;
+        O2Args oa;
+        oa.state = state + off;
+        oa.S = ob.S + off;
+        oa.flag = ob.flag + off;
+        oa.active = ob.active ? ob.active + off : nullptr;
+        oa.limit_mode = ob.limit_mode;
+        oa.ctrl = ctrl;
+        oa.stage = stage;
+        const int x = seg * SEG - 1 + lane;
+        if (lane < 1 || lane > SEG || x >= gp.n[0]) return;
+        const int y1 = min((chunk + 1) * gp.chunk, gp.n[1]);
+        for (int y = chunk * gp.chunk; y < y1; ++y) slopes_cell<A, 2>(gp, oa, (long long)x + (long long)gp.n[0] * y);
+    });
+}
+
+// W1 = U + dt R1 / V of the output cells of every item (per-case dt)
+template <class A>
+__global__ void __launch_bounds__(128) form_w1_batch_kernel(const CaseDesc *__restrict__ cases,
+                                                            const int *__restrict__ item_case, int nitems, Ctrl *cctrl,
+                                                            StageArgs base, double *W1)
+{
+    const int lane = threadIdx.x & 31;
+    for_items(cases, item_case, nitems, cctrl, [&](const GridParams &gp, long long off, Ctrl *ctrl, int seg, int chunk,
+                                                   bool first) {
+        const StepScalars sc = step_scalars<A, STAGE_2>(gp, ctrl);
+        if (first && lane == 0 && sc.active) ctrl->dt = sc.dt;
+        if (!sc.active) return;
+        StageArgs sa = base;
+        sa.U = base.U + off;
+        sa.R = base.R + off;
+        const int x = seg * SEG - 1 + lane;
+        if (lane < 1 || lane > SEG || x >= gp.n[0]) return;
+        const int y1 = min((chunk + 1) * gp.chunk, gp.n[1]);
+        for (int y = chunk * gp.chunk; y < y1; ++y) {
+            const long long g = (long long)x + (long long)gp.n[0] * y;
+#pragma unroll
+            for (int k = 0; k < A::NVAR; ++k) {
+                const long long o = (long long)A::field(k) * gp.plane + g;
+                W1[off + o] = form_w1_value<A>(sa, gp, sc, o);
+            }
+        }
+    });
+}
+
+// order-2 stage march of every item
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_o2_batch_kernel(const CaseDesc *__restrict__ cases,
+                                                               const int *__restrict__ item_case, int nitems,
+                                                               Ctrl *cctrl, StageArgs base, const double *state,
+                                                               const double *S)
+{
+    const int lane = threadIdx.x & 31;
+    for_items(cases, item_case, nitems, cctrl, [&](const GridParams &gp, long long off, Ctrl *ctrl, int seg, int chunk,
+                                                   bool first) {
+        const StepScalars sc = step_scalars<A, STAGE>(gp, ctrl);
+        if (first && lane == 0) step_bookkeeping<STAGE>(ctrl, sc);
+        if (!sc.active) return;
+        StageArgs sa = base;
+        sa.U = base.U + off;
+        sa.R = base.R + off;
+        sa.W = base.W + off;
+        sa.out = base.out + off;
+        sa.ctrl = ctrl;
+        double lmax = 0.0;
+        unsigned status = 0;
+        march2d_o2<A, STAGE>(gp, sa, state + off, S + off, sc, seg, chunk, lmax, status);
+        publish_reductions<STAGE>(lmax, status, ctrl, nullptr);
+    });
+}
+
+enum BatchO2Op { BO2_SLOPES = 0, BO2_FORM_W1 = 1, BO2_STAGE = 2 };
+
+template <class A>
+inline cudaError_t launch_batch_o2(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
+                                   Ctrl *cctrl, const StageArgs &base, const double *state, const O2Batch &ob,
+                                   double *W1, int blocks, cudaStream_t s)
+{
+    switch (op) {
+    case BO2_SLOPES: slopes_batch_kernel<A><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, state, ob, stage); break;
+    case BO2_FORM_W1: form_w1_batch_kernel<A><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base, W1); break;
+    case BO2_STAGE:
+        switch (stage) {
+        case STAGE_1: stage2d_o2_batch_kernel<A, STAGE_1><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base, state, ob.S); break;
+        case STAGE_2: stage2d_o2_batch_kernel<A, STAGE_2><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base, state, ob.S); break;
+        case STAGE_3: stage2d_o2_batch_kernel<A, STAGE_3><<<blocks, 128, 0, s>>>(cases, item_case, nitems, cctrl, base, state, ob.S); break;
+        default: return cudaErrorInvalidValue;
+        }
+        break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaPeekAtLastError();
+}
+
+cudaError_t launch_batch_o2_exact(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
+                                  Ctrl *cctrl, const StageArgs &base, const double *state, const O2Batch &ob,
+                                  double *W1, int blocks, cudaStream_t s);
+cudaError_t launch_batch_o2_fast(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
+                                 Ctrl *cctrl, const StageArgs &base, const double *state, const O2Batch &ob,
+                                 double *W1, int blocks, cudaStream_t s, bool w_zero);
 
 // Entry points (arithmetic translation units).
 cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,

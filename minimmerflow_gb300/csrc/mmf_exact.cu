@@ -18,6 +18,13 @@ cudaError_t launch_o2_exact(int op, int stage, const GridParams &gp, const Stage
     return launch_o2<ExactArith>(op, stage, gp, sa, oa, W1, s);
 }
 
+cudaError_t launch_batch_o2_exact(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
+                                  Ctrl *cctrl, const StageArgs &base, const double *state, const O2Batch &ob,
+                                  double *W1, int blocks, cudaStream_t s)
+{
+    return launch_batch_o2<ExactArith>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
+}
+
 int batch_max_blocks_per_sm_exact() { return batch_blocks_per_sm<ExactArith>(); }
 
 cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,

@@ -26,6 +26,15 @@ cudaError_t launch_batch_fast(int stage, const CaseDesc *cases, const int *item_
     return launch_batch<FastArith>(stage, cases, item_case, nitems, cctrl, base, blocks, s);
 }
 
+cudaError_t launch_batch_o2_fast(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
+                                 Ctrl *cctrl, const StageArgs &base, const double *state, const O2Batch &ob,
+                                 double *W1, int blocks, cudaStream_t s, bool w_zero)
+{
+    if (w_zero)
+        return launch_batch_o2<FastArith2DW0>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
+    return launch_batch_o2<FastArith>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
+}
+
 int batch_max_blocks_per_sm(int arith, bool w_zero)
 {
     if (arith == 0) return batch_max_blocks_per_sm_exact();

@@ -46,12 +46,12 @@ static int mlp_pack(mmf_mlp *p)
     return MMF_OK;
 }
 
-template <int DIM, bool FROM_X>
+template <int DIM, int SRC>
 static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const double *U, const __nv_bfloat16 *X, float thr,
-                                float *prob, unsigned char *flags, cudaStream_t s)
+                                float *prob, unsigned char *flags, cudaStream_t s, BatchGeom bg = BatchGeom{nullptr, nullptr, 0})
 {
     const int smem = mlp_infer_smem<DIM>();
-    cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel<DIM, FROM_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel<DIM, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
@@ -62,7 +62,7 @@ static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const double *
     w.w1c = p->w1c;
     w.w2c = p->w2c;
     w.params = p->params;
-    mlp_infer_kernel<DIM, FROM_X><<<blocks, 128, smem, s>>>(gp, U, X, w, thr, prob, flags, p->err);
+    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, U, X, w, thr, prob, flags, p->err, bg);
     return cudaPeekAtLastError();
 }
 
@@ -71,8 +71,20 @@ cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, flo
                           unsigned char *flags, cudaStream_t s)
 {
     if (p->dim != gp.dim) return cudaErrorInvalidValue;
-    return p->dim == 3 ? launch_infer<3, false>(p, gp, U, nullptr, thr, prob, flags, s)
-                       : launch_infer<2, false>(p, gp, U, nullptr, thr, prob, flags, s);
+    return p->dim == 3 ? launch_infer<3, MLP_SRC_GRID>(p, gp, U, nullptr, thr, prob, flags, s)
+                       : launch_infer<2, MLP_SRC_GRID>(p, gp, U, nullptr, thr, prob, flags, s);
+}
+
+// Indicator over a packed batch of 2D grids (total cells).
+cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
+                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s)
+{
+    if (p->dim != 2) return cudaErrorInvalidValue;
+    GridParams gp;
+    memset(&gp, 0, sizeof(gp));
+    gp.dim = 2;
+    gp.plane = total;
+    return launch_infer<2, MLP_SRC_BATCH>(p, gp, U, nullptr, thr, nullptr, flags, s, BatchGeom{cases, offsets, ncases});
 }
 
 cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s)
@@ -240,8 +252,8 @@ int mmf_mlp_predict(mmf_mlp *p, const void *d_X, int64_t n, float *d_prob)
     gp.dim = p->dim;
     gp.plane = n;
     MLP_CUDA(cudaMemsetAsync(p->err, 0, sizeof(int), p->stream));
-    cudaError_t e = (p->dim == 3) ? launch_infer<3, true>(p, gp, nullptr, (const __nv_bfloat16 *)d_X, 0.5f, d_prob, nullptr, p->stream)
-                                  : launch_infer<2, true>(p, gp, nullptr, (const __nv_bfloat16 *)d_X, 0.5f, d_prob, nullptr, p->stream);
+    cudaError_t e = (p->dim == 3) ? launch_infer<3, MLP_SRC_X>(p, gp, nullptr, (const __nv_bfloat16 *)d_X, 0.5f, d_prob, nullptr, p->stream)
+                                  : launch_infer<2, MLP_SRC_X>(p, gp, nullptr, (const __nv_bfloat16 *)d_X, 0.5f, d_prob, nullptr, p->stream);
     MLP_CUDA(e);
     MLP_CUDA(cudaStreamSynchronize(p->stream));
     if (mlp_error(p)) return set_last_error(MMF_ERR_CUDA, "MLP kernel: an asynchronous-copy or MMA wait gave up");

@@ -33,7 +33,7 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 
-#include "mmf_cartesian.cuh"
+#include "mmf_batch.cuh"
 
 namespace mmf {
 
@@ -174,6 +174,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+// Cells of a packed batch of 2D grids: case c covers [offsets[c], offsets[c+1]).
+struct BatchGeom {
+    const CaseDesc *cases;
+    const long long *offsets;
+    int ncases;
+};
+
+__device__ __forceinline__ int case_of(const BatchGeom &bg, long long g)
+{
+    int lo = 0, hi = bg.ncases - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bg.offsets[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+enum { MLP_SRC_GRID = 0, MLP_SRC_X = 1, MLP_SRC_BATCH = 2 };
+
 struct MlpDev {
     const __nv_bfloat16 *w1c;   // W1 in the operand layout, 64 rows x KPAD
     const __nv_bfloat16 *w2c;   // W2 in the operand layout, 64 rows x 64
@@ -183,10 +202,10 @@ struct MlpDev {
 // Fused features + MLP over the cells of a grid (persistent, one 128-cell tile
 // per iteration).  prob (nullable) receives y, flags (nullable) y > threshold.
 // Returns through *err a non-zero code if an MMA completion wait gave up.
-template <int DIM, bool FROM_X>
+template <int DIM, int SRC>
 __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const double *U, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
-                                                           unsigned char *flags, int *err)
+                                                           unsigned char *flags, int *err, BatchGeom bg)
 {
     constexpr int KP = mlp_kpad(DIM);
     extern __shared__ __align__(1024) unsigned char dyn[];
@@ -244,8 +263,13 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     for (long long tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
         const long long g = tile * MLP_TILE + tid;
         // features of this thread's cell -> BF16 operand rows
-        if (g < gp.plane && FROM_X) {
+        if (g < gp.plane && SRC == MLP_SRC_X) {
             for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = X[g * KP + k];
+        } else if (g < gp.plane && SRC == MLP_SRC_BATCH) {
+            const int c = case_of(bg, g);
+            const long long off = bg.offsets[c];
+            cell_features<DIM>(U + off, bg.cases[c].gp, g - off,
+                               [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
         } else if (g < gp.plane) {
             cell_features<DIM>(U, gp, g, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
         } else {

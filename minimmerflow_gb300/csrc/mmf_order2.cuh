@@ -78,86 +78,103 @@ __device__ __forceinline__ void load_plain(const double *planes, long long plane
     for (int k = 0; k < A::NVAR; ++k) c[k] = __ldg(planes + (long long)A::field(k) * plane + g);
 }
 
-// computePolynomials: one thread per cell (grid-stride).
+// computePolynomials of grid cell g (index inside the grid; field planes of
+// the grid are gp.plane apart).
+template <class A, int DIM>
+__device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &oa, long long g)
+{
+    constexpr int NV = A::NVAR;
+    const int nx = gp.n[0], ny = gp.n[1];
+    const long long n = gp.plane;
+    const int ix = (int)(g % nx);
+    const int iy = (int)((g / nx) % ny);
+    const int iz = (DIM == 3) ? (int)(g / ((long long)nx * ny)) : 0;
+    const int idx[3] = {ix, iy, iz};
+    double uc[NV];
+    load_plain<A>(oa.state, n, g, uc);
+    const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
+    bool act = false;
+    double sig[DIM][NV];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        double ul[NV], ur[NV];
+        for (int s = 0; s < 2; ++s) {
+            double *u = s ? ur : ul;
+            const int q = idx[d] + (s ? 1 : -1);
+            const bool per = gp.bc_lo[d] == BC_PERIODIC;
+            const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
+            if (q >= 0 && q < gp.n[d]) {
+                load_plain<A>(oa.state, n, g + (s ? stride : -stride), u);
+            } else if (per) {
+                const long long wrap = (long long)(gp.n[d] - 1) * stride;
+                load_plain<A>(oa.state, n, s ? g - wrap : g + wrap, u);
+            } else {
+                double nrm[3] = {0.0, 0.0, 0.0};
+                nrm[d] = s ? 1.0 : -1.0;
+                ghost_state<A>(s ? gp.bc_hi[d] : gp.bc_lo[d], nrm, uc, gp.dir_prim, u);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double a = uc[k] - ul[k];
+            const double b = ur[k] - uc[k];
+            const double central = 0.5 * (a + b);
+            double sl = central;
+            if (limit) {
+                sl = mc_slope<A>(a, b, central);
+                if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
+            }
+            sig[d][k] = sl;
+        }
+    }
+    if (limit || oa.limit_mode == LIMIT_FLAGGED) {
+        // positivity fallback, also for the cells a flag leaves on central slopes
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            double fm[NV], fp[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { fm[k] = uc[k] - 0.5 * sig[d][k]; fp[k] = uc[k] + 0.5 * sig[d][k]; }
+            ok = ok && admissible<A>(fm) && admissible<A>(fp);
+        }
+        if (!ok) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sig[d][k] = 0.0;
+            act = true;
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = sig[d][k];
+    if (oa.active) oa.active[g] = act ? 1 : 0;
+}
+
+__device__ __forceinline__ bool o2_step_active(const Ctrl *ctrl, int stage)
+{
+    if (stage < 1) return true;
+    return (stage == 1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps) : ctrl->active != 0;
+}
+
+// computePolynomials over a grid: one thread per cell (grid-stride).
 template <class A, int DIM>
 __global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
 {
-    constexpr int NV = A::NVAR;
-    if (oa.stage >= 1) {
-        const Ctrl *ctrl = oa.ctrl;
-        const bool active = (oa.stage == 1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps)
-                                            : ctrl->active != 0;
-        if (!active) return;
-    }
-    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
-    const long long n = gp.plane;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
-         g += (long long)gridDim.x * blockDim.x) {
-        const int ix = (int)(g % nx);
-        const int iy = (int)((g / nx) % ny);
-        const int iz = (DIM == 3) ? (int)(g / ((long long)nx * ny)) : 0;
-        const int idx[3] = {ix, iy, iz};
-        double uc[NV];
-        load_plain<A>(oa.state, n, g, uc);
-        const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
-        bool act = false;
-        double sig[DIM][NV];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            double ul[NV], ur[NV];
-            for (int s = 0; s < 2; ++s) {
-                double *u = s ? ur : ul;
-                const int q = idx[d] + (s ? 1 : -1);
-                const bool per = gp.bc_lo[d] == BC_PERIODIC;
-                if (q >= 0 && q < gp.n[d]) {
-                    const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
-                    load_plain<A>(oa.state, n, g + (s ? stride : -stride), u);
-                } else if (per) {
-                    const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
-                    const long long wrap = (long long)(gp.n[d] - 1) * stride;
-                    load_plain<A>(oa.state, n, s ? g - wrap : g + wrap, u);
-                } else {
-                    double nrm[3] = {0.0, 0.0, 0.0};
-                    nrm[d] = s ? 1.0 : -1.0;
-                    ghost_state<A>(s ? gp.bc_hi[d] : gp.bc_lo[d], nrm, uc, gp.dir_prim, u);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                const double a = uc[k] - ul[k];
-                const double b = ur[k] - uc[k];
-                const double central = 0.5 * (a + b);
-                double sl = central;
-                if (limit) {
-                    sl = mc_slope<A>(a, b, central);
-                    if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
-                }
-                sig[d][k] = sl;
-            }
-        }
-        if (limit) {
-            bool ok = true;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                double fm[NV], fp[NV];
-#pragma unroll
-                for (int k = 0; k < NV; ++k) { fm[k] = uc[k] - 0.5 * sig[d][k]; fp[k] = uc[k] + 0.5 * sig[d][k]; }
-                ok = ok && admissible<A>(fm) && admissible<A>(fp);
-            }
-            if (!ok) {
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-#pragma unroll
-                    for (int k = 0; k < NV; ++k) sig[d][k] = 0.0;
-                act = true;
-            }
-        }
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-#pragma unroll
-            for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = sig[d][k];
-        if (oa.active) oa.active[g] = act ? 1 : 0;
-    }
+    if (!o2_step_active(oa.ctrl, oa.stage)) return;
+    const long long cells = (long long)gp.n[0] * gp.n[1] * gp.n[2];
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < cells;
+         g += (long long)gridDim.x * blockDim.x)
+        slopes_cell<A, DIM>(gp, oa, g);
+}
+
+template <class A>
+__device__ __forceinline__ double form_w1_value(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                                long long o)
+{
+    const double u = __ldg(sa.U + o), r = __ldg(sa.R + o);
+    return IsExact<A>::value ? u + sc.dt * r / gp.vol : fma(sc.s, r, u);
 }
 
 // W1 = U + dt R1 / V (stage 2 input), with the stage-2 dt bookkeeping.
@@ -171,8 +188,7 @@ __global__ void __launch_bounds__(256) form_w1_kernel(GridParams gp, StageArgs s
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)A::NVAR * n;
          i += (long long)gridDim.x * blockDim.x) {
         const long long o = (long long)A::field((int)(i / n)) * n + i % n;
-        const double u = __ldg(sa.U + o), r = __ldg(sa.R + o);
-        W1[o] = IsExact<A>::value ? u + sc.dt * r / gp.vol : fma(sc.s, r, u);
+        W1[o] = form_w1_value<A>(sa, gp, sc, o);
     }
 }
 
@@ -298,29 +314,22 @@ __device__ __forceinline__ void store_output_o2(const StageArgs &sa, const GridP
 }
 
 // ---------------------------------------------------------------- 2D, order 2
+// One warp's work item (as march2d, with face-side records).
 template <class A, int STAGE>
-__global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArgs sa, const double *state,
-                                                         const double *S)
+__device__ __forceinline__ void march2d_o2(const GridParams &gp, const StageArgs &sa, const double *state,
+                                           const double *S, const StepScalars &sc, int seg, int chunk, double &lmax,
+                                           unsigned &status)
 {
     constexpr int NV = A::NVAR;
     const int lane = threadIdx.x & 31;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (warp >= gp.nseg * gp.nchunk) return;
-    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
-    if (!sc.active) return;
-
     const int nx = gp.n[0], ny = gp.n[1];
-    const int seg = warp % gp.nseg, chunk = warp / gp.nseg;
     const int x = seg * SEG - 1 + lane;
     const int y0 = chunk * gp.chunk;
     const int y1 = min(y0 + gp.chunk, ny);
     const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
     const bool xface_valid = (lane <= SEG) && (x < nx);
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC;
-    unsigned status = 0;
     unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
-    double lmax = 0.0;
 
     SideRec<A, 2> cur, abv;
     double Fylo[NV], Fyhi[NV], Fxlo[NV], Fxhi[NV], acc[NV];
@@ -345,18 +354,21 @@ __global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArg
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fylo[k] = Fyhi[k];
     }
-    if (STAGE <= STAGE_1) {
-        lmax = warp_max(lmax);
-        if (lane == 0) {
-            unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
-                                                           : &sa.ctrl->maxeig_bits;
-            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
-        }
-        if (STAGE == STAGE_1) {
-            status = __reduce_or_sync(0xffffffffu, status);
-            if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
-        }
-    }
+}
+
+template <class A, int STAGE>
+__global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArgs sa, const double *state,
+                                                         const double *S)
+{
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (warp >= gp.nseg * gp.nchunk) return;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+    double lmax = 0.0;
+    unsigned status = 0;
+    march2d_o2<A, STAGE>(gp, sa, state, S, sc, warp % gp.nseg, warp / gp.nseg, lmax, status);
+    publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }
 
 // ---------------------------------------------------------------- 3D, order 2

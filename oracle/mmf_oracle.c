@@ -464,8 +464,9 @@ void orc_compute_polynomials(const orc_mesh *m, int problem, int order, const do
                 sd[k] = s;
             }
         }
-        if (limit) {
-            /* positivity fallback: every face state must stay admissible */
+        if (limit || limiter_mode == 2) {
+            /* positivity fallback: every face state must stay admissible (also
+             * for the cells a flag leaves on central slopes) */
             int ok = 1;
             for (int d = 0; d < m->dim && ok; ++d) {
                 const double *sd = slopes + (c * 3 + d) * NF;

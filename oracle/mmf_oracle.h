@@ -117,7 +117,8 @@ void orc_mesh_free(orc_mesh *m);
 /* ---- reconstruction (reconstruction.cpp:47-97).  Order 1 is the reference
  * (copy of the mean).  EXTENSION: order 2 = MUSCL slopes per direction with
  * the monotonised-central (MC) limiter; 'limiter_mode' 0 = limit every cell,
- * 1 = never limit (central slopes), 2 = limit only cells with flag[c] != 0.
+ * 1 = never limit (central slopes), 2 = limit only cells with flag[c] != 0
+ * (the others take central slopes but keep the positivity fallback).
  * 'active' (nullable) receives 1 where the limiter changed a slope by more
  * than 1e-6 (|rho| + |rho E|) of the cell, or fell back to order 1. */
 void orc_compute_polynomials(const orc_mesh *m, int problem, int order, const double *U,

@@ -68,3 +68,42 @@ def test_autotune_keeps_state(mmf):
         plain = b.run(states, 6)
     for x, y in zip(tuned, plain):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("arith", ["fast", "reference"])
+def test_batch_order2_equals_single_contexts(mmf, arith):
+    from minimmerflow_gb300.batch import BatchEuler
+    cases = small_sweep(mmf, ncases=8, seed=21)
+    for c in cases:
+        c.cfl = 0.4
+    states = [c.initial_state() for c in cases]
+    with BatchEuler(cases, arith=arith, order=2) as b:
+        out = b.run(states, 10)
+    for i, (c, U0) in enumerate(zip(cases, states)):
+        with c.solver(arith=arith, order=2) as s:
+            U, t, n = s.run(U0, c.cfl, max_steps=10)
+        assert np.array_equal(out[i], U), c.name
+
+
+def test_batch_order2_with_indicator_equals_single_contexts(mmf):
+    """The learned indicator inside the batch gives every case the flags (and so
+    the state) of its own single-case run with the same indicator."""
+    from minimmerflow_gb300 import indicator
+    from minimmerflow_gb300.batch import BatchEuler
+    mlp = indicator.TroubledCellMLP(dim=2, seed=4)
+    p = mlp.params()
+    p[-1] = 0.0   # b3: roughly half the cells flagged by the random network
+    mlp.set_params(p)
+    # vortices only: a random (untrained) network leaves shock cells unlimited
+    cases = [c for c in small_sweep(mmf, ncases=12, seed=22) if c.problem == mmf.problem.VORTEX_XY]
+    for c in cases:
+        c.cfl = 0.4
+    states = [c.initial_state() for c in cases]
+    with BatchEuler(cases, arith="fast", order=2) as b:
+        b.set_indicator(mlp, 0.5)
+        out = b.run(states, 6)
+    for i, (c, U0) in enumerate(zip(cases, states)):
+        with c.solver(arith="fast", order=2) as s:
+            indicator.use_indicator(s, mlp, 0.5)
+            U, t, n = s.run(U0, c.cfl, max_steps=6)
+        assert np.array_equal(out[i], U), c.name
