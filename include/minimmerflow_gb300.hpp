@@ -14,8 +14,10 @@
  * the same code binds to bitpit's MeshGeometricalInfo / PiercedStorage in
  * minimmerflow (or to any type with the same methods):
  *   MeshInfo:    getDimension(), getCellRawIds(), rawGetCellCentroid(raw),
- *                rawGetCellSize(raw), getInterfaceRawIds(), rawGetInterfaceNormal(raw),
- *                getPatch().getInterfaces().rawAt(raw).getNeigh()
+ *                rawGetCellSize(raw), rawGetCellVolume(raw), getInterfaceRawIds(),
+ *                rawGetInterfaceNormal(raw), rawGetInterfaceArea(raw),
+ *                getPatch().getInterfaces().rawAt(raw).{getOwner,getNeigh}(),
+ *                getPatch().getCellConstIterator(id).getRawIndex()
  *   Storages:    rawData(raw) (AoS, contiguous over the raw positions), rawAt(raw)
  *
  * Error behaviour follows the reference: unsupported configurations throw
@@ -157,6 +159,101 @@ void releaseContext(const MeshInfo &meshInfo)
     detail::contexts<MeshInfo>().erase(&meshInfo);
 }
 
+/* A face-list context (mmf_umesh) bound to one mesh: any MeshGeometricalInfo
+ * -- non-uniform / refined meshes, immersed bodies, per-face border
+ * conditions.  Raw ids with holes are kept: the state buffer is indexed by
+ * raw position and the holes are unsolved cells without faces. */
+class UContext {
+public:
+    template <class MeshInfo, class CellStorageBool, class InterfaceStorageInt>
+    UContext(const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, const InterfaceStorageInt &interfaceBCs,
+             int arith, int device = 0)
+    {
+        const std::vector<std::size_t> &cells = meshInfo.getCellRawIds();
+        std::size_t n = 0;
+        for (std::size_t raw : cells) n = std::max(n, raw + 1);
+        std::vector<double> vol(n, 1.0), size(n, std::numeric_limits<double>::max());
+        std::vector<unsigned char> solved(n, 0);
+        for (std::size_t raw : cells) {
+            vol[raw] = meshInfo.rawGetCellVolume(raw);
+            size[raw] = meshInfo.rawGetCellSize(raw);
+            solved[raw] = cellSolvedFlag.rawAt(raw) ? 1 : 0;
+        }
+        const std::vector<std::size_t> &faces = meshInfo.getInterfaceRawIds();
+        std::vector<int64_t> owner, neigh;
+        std::vector<double> area, normal;
+        std::vector<int> bc;
+        for (std::size_t raw : faces) {   // src/euler.cpp:153-178: the face loop and its id -> raw lookups
+            const auto &itf = meshInfo.getPatch().getInterfaces().rawAt(raw);
+            owner.push_back((int64_t)meshInfo.getPatch().getCellConstIterator(itf.getOwner()).getRawIndex());
+            const long nid = itf.getNeigh();
+            neigh.push_back(nid >= 0 ? (int64_t)meshInfo.getPatch().getCellConstIterator(nid).getRawIndex() : -1);
+            area.push_back(meshInfo.rawGetInterfaceArea(raw));
+            const std::array<double, 3> &nr = meshInfo.rawGetInterfaceNormal(raw);
+            normal.insert(normal.end(), nr.begin(), nr.end());
+            bc.push_back((int)interfaceBCs.rawAt(raw));
+        }
+        mmf_umesh_desc d;
+        d.dim = meshInfo.getDimension();
+        d.n_cells = (int64_t)n;
+        d.n_faces = (int64_t)owner.size();
+        d.cell_volume = vol.data();
+        d.cell_size = size.data();
+        d.solved = solved.data();
+        d.owner = owner.data();
+        d.neigh = neigh.data();
+        d.area = area.data();
+        d.normal = normal.data();
+        d.bc = bc.data();
+        for (int k = 0; k < 5; ++k) d.dirichlet_prim[k] = 0.0;
+        d.arith = arith;
+        check(mmf_umesh_create(&d, device, &m_u));
+        m_n = (int64_t)n;
+    }
+    ~UContext() { mmf_umesh_destroy(m_u); }
+    UContext(const UContext &) = delete;
+    UContext &operator=(const UContext &) = delete;
+    mmf_umesh *get() const { return m_u; }
+    int64_t nCells() const { return m_n; }
+
+private:
+    mmf_umesh *m_u = nullptr;
+    int64_t m_n = 0;
+};
+
+namespace detail {
+template <class Key>
+std::map<const void *, std::unique_ptr<UContext>> &ucontexts()
+{
+    static std::map<const void *, std::unique_ptr<UContext>> m;
+    return m;
+}
+
+/* true when the mesh is a full uniform grid with one border condition per side
+ * and every cell is solved: the Cartesian kernels apply */
+template <class MeshInfo, class CellStorageBool, class InterfaceStorageInt>
+bool cartesian_applies(const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag,
+                       const InterfaceStorageInt &interfaceBCs)
+{
+    for (std::size_t raw : meshInfo.getCellRawIds())
+        if (!cellSolvedFlag.rawAt(raw)) return false;
+    try {
+        std::vector<int64_t> map;
+        describeGrid(meshInfo, interfaceBCs, 1, MMF_ARITH_REFERENCE, &map);
+    } catch (const std::runtime_error &) {
+        return false;
+    }
+    return true;
+}
+}
+
+template <class MeshInfo>
+void releaseContexts(const MeshInfo &meshInfo)
+{
+    detail::contexts<MeshInfo>().erase(&meshInfo);
+    detail::ucontexts<MeshInfo>().erase(&meshInfo);
+}
+
 namespace reconstruction {
 /* reconstruction::computePolynomials (src/reconstruction.cpp:47-55): order 1
  * needs no polynomial data. */
@@ -172,16 +269,28 @@ void computePolynomials(ProblemType, const MeshInfo &meshInfo, const CellStorage
 namespace euler {
 /* euler::computeRHS (src/euler.cpp:127-249): residual (not divided by the
  * volume) of every cell of 'cellConservatives' into 'cellsRHS', and the
- * maximum face eigenvalue.  Every cell must be solved (no immersed bodies). */
+ * maximum face eigenvalue.  A full uniform grid with every cell solved runs
+ * on the Cartesian kernels; any other mesh (refined, immersed bodies, per-face
+ * border conditions) on the face-list kernels.  Both use the reference
+ * arithmetic: the result equals the reference's bit for bit. */
 template <class ProblemType, class MeshInfo, class CellStorageBool, class CellStorageDouble, class InterfaceStorageInt>
 void computeRHS(ProblemType, const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, int order,
                 const CellStorageDouble &cellConservatives, const InterfaceStorageInt &interfaceBCs,
                 CellStorageDouble *cellsRHS, double *maxEig)
 {
-    if (order != 1) throw std::runtime_error("mmf_gb300: only order 1 is supported");
+    if (order != 1) throw std::runtime_error("mmf_gb300: only order 1 is supported by this entry point");
+    auto &um = detail::ucontexts<MeshInfo>();
+    auto uit = um.find(&meshInfo);
+    if (uit == um.end() && detail::contexts<MeshInfo>().count(&meshInfo) == 0 &&
+        !detail::cartesian_applies(meshInfo, cellSolvedFlag, interfaceBCs))
+        uit = um.emplace(&meshInfo, std::unique_ptr<UContext>(new UContext(meshInfo, cellSolvedFlag, interfaceBCs,
+                                                                           MMF_ARITH_REFERENCE))).first;
+    if (uit != um.end()) {
+        check(mmf_umesh_compute_rhs(uit->second->get(), cellConservatives.rawData(0), cellsRHS->rawData(0), maxEig,
+                                    uit->second->nCells()));
+        return;
+    }
     Context &ctx = contextFor(meshInfo, interfaceBCs, order);
-    for (std::size_t raw : meshInfo.getCellRawIds())
-        if (!cellSolvedFlag.rawAt(raw)) throw std::runtime_error("mmf_gb300: unsolved cells are not supported");
     check(mmf_compute_rhs(ctx.get(), cellConservatives.rawData(0), cellsRHS->rawData(0), maxEig, ctx.nCells()));
 }
 

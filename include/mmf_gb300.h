@@ -157,6 +157,38 @@ int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, co
 int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
                        const double *dirichlet_prim, double *cons_bc);
 
+/* ---- general face lists ------------------------------------------------ */
+/* The Euler step on any mesh given as MeshGeometricalInfo-like arrays
+ * (src/mesh_info.hpp:31-105): per raw cell volume, size and solved flag
+ * (cellSolvedFlag), per interface owner / neighbour raw ids (neighbour -1 on a
+ * border), area, normal [n_faces][3] (owner -> neighbour) and border
+ * condition (interfaceBCs; MMF_BC_NONE inside, MMF_BC_WALL between fluid and
+ * solid cells, src/main.cpp:251-277).  The residual keeps the reference's face
+ * order (src/euler.cpp:153-248) through an atomic-free per-cell gather, so the
+ * reference arithmetic is bit-identical on any mesh: refined octrees,
+ * immersed bodies, the forward-facing step.  Order 1. */
+typedef struct {
+    int dim;
+    int64_t n_cells, n_faces;
+    const double *cell_volume, *cell_size;
+    const unsigned char *solved;    /* NULL = every cell solved */
+    const int64_t *owner, *neigh;
+    const double *area, *normal;
+    const int *bc;
+    double dirichlet_prim[5];       /* (p,u,v,w,T) behind MMF_BC_DIRICHLET faces */
+    int arith;
+} mmf_umesh_desc;
+typedef struct mmf_umesh mmf_umesh;
+int mmf_umesh_create(const mmf_umesh_desc *desc, int device, mmf_umesh **out);
+int mmf_umesh_destroy(mmf_umesh *u);
+int64_t mmf_umesh_launch_count(const mmf_umesh *u);
+int mmf_umesh_upload(mmf_umesh *u, const double *aos, int64_t n_cells);
+int mmf_umesh_download(mmf_umesh *u, double *aos, int64_t n_cells);
+/* euler::computeRHS on the face list (residual not divided by the volume). */
+int mmf_umesh_compute_rhs(mmf_umesh *u, const double *cons, double *rhs, double *max_eig, int64_t n_cells);
+int mmf_umesh_time_setup(mmf_umesh *u, double cfl, double t, double t_end, int64_t max_steps);
+int mmf_umesh_advance(mmf_umesh *u, int64_t n_steps, double *t_out, int64_t *steps_done);
+
 /* ---- batched cases ------------------------------------------------------ */
 /* Many independent 2D cases of uneven size advanced together: one
  * persistent launch per RK stage walks a list of (case, segment, row chunk)

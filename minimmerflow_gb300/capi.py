@@ -29,6 +29,8 @@ EXPORTS = [
     "mmf_mlp_create", "mmf_mlp_destroy", "mmf_mlp_num_params", "mmf_mlp_input_width", "mmf_mlp_get_params",
     "mmf_mlp_set_params", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
     "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
+    "mmf_umesh_create", "mmf_umesh_destroy", "mmf_umesh_launch_count", "mmf_umesh_upload", "mmf_umesh_download",
+    "mmf_umesh_compute_rhs", "mmf_umesh_time_setup", "mmf_umesh_advance",
 ]
 LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
@@ -38,6 +40,13 @@ class Grid(C.Structure):
     _fields_ = [("dim", C.c_int), ("n", C.c_int * 3), ("origin", C.c_double * 3), ("h", C.c_double),
                 ("bc_lo", C.c_int * 3), ("bc_hi", C.c_int * 3), ("dirichlet_prim", C.c_double * 5),
                 ("order", C.c_int), ("arith", C.c_int), ("chunk", C.c_int)]
+
+
+class UMeshDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("n_cells", C.c_int64), ("n_faces", C.c_int64),
+                ("cell_volume", C.c_void_p), ("cell_size", C.c_void_p), ("solved", C.c_void_p),
+                ("owner", C.c_void_p), ("neigh", C.c_void_p), ("area", C.c_void_p), ("normal", C.c_void_p),
+                ("bc", C.c_void_p), ("dirichlet_prim", C.c_double * 5), ("arith", C.c_int)]
 
 
 class MMFError(RuntimeError):
@@ -124,6 +133,15 @@ def load(build_if_missing=True):
     L.mmf_indicator.argtypes = [_P, _P, C.c_float, _P, _P]
     L.mmf_set_indicator.argtypes = [_P, _P, C.c_float]
     L.mmf_limiter_labels.argtypes = [_P, _P]
+    L.mmf_umesh_create.argtypes = [C.POINTER(UMeshDesc), C.c_int, C.POINTER(_P)]
+    L.mmf_umesh_destroy.argtypes = [_P]
+    L.mmf_umesh_launch_count.argtypes = [_P]
+    L.mmf_umesh_launch_count.restype = C.c_int64
+    L.mmf_umesh_upload.argtypes = [_P, _P, C.c_int64]
+    L.mmf_umesh_download.argtypes = [_P, _P, C.c_int64]
+    L.mmf_umesh_compute_rhs.argtypes = [_P, _P, _P, _D, C.c_int64]
+    L.mmf_umesh_time_setup.argtypes = [_P, C.c_double, C.c_double, C.c_double, C.c_int64]
+    L.mmf_umesh_advance.argtypes = [_P, C.c_int64, _D, C.POINTER(C.c_int64)]
     L.mmf_compute_rhs_noalloc.argtypes = [C.POINTER(Grid), _P, _P, _P, _P, _P]
     _lib = L
     return L

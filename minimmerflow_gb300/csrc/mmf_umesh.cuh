@@ -1,0 +1,217 @@
+// mmf_umesh.cuh -- the Euler step on a general face list: the structure of
+// MeshGeometricalInfo (mesh_info.hpp:31-105) with per-face border conditions
+// and per-cell solved flags, i.e. the reference's computeRHS
+// (euler.cpp:127-249) on any mesh -- refined octrees, immersed bodies
+// (BC_WALL faces between fluid and solid cells, main.cpp:251-277), the
+// forward-facing step's Dirichlet / free-flow / reflecting borders.
+//
+//   uface_kernel   one thread per interface: the face states (order 1: the
+//                  cell means; a border or wall face: the ghost of the fluid
+//                  side with the normal flipped when the neighbour is the
+//                  fluid, euler.cpp:197-226), the LLF flux, P_f = area * F
+//                  (5 planes over the faces), the face max eigenvalue.
+//   ucell_kernel   one thread per cell: the residual R = sum of -P_f (owner)
+//                  and +P_f (neighbour) over the cell's faces in face-list
+//                  order (a CSR list built on the host, so the sum is the
+//                  reference's, atomic-free), then the stage combination.
+//   uform_w1       W1 = U + dt R1 / V materialised for stage 2.
+//
+// State planes are indexed by raw id; unsolved cells keep their state and get
+// no residual, as in the reference.
+#pragma once
+
+#include "mmf_cartesian.cuh"
+
+namespace mmf {
+
+struct UMesh {
+    long long ncells, nfaces;
+    const double *vol;            // per cell
+    const unsigned char *solved;  // per cell
+    const long long *owner, *neigh;
+    const double *area;           // per face
+    const double *normal;         // 3 planes over the faces
+    const int *bc;                // per face (BC_NONE interior)
+    const long long *csr_off;     // per cell: [off[c], off[c+1]) into csr_face
+    const long long *csr_face;    // face index, negated - 1 when the cell is the owner
+    double dir_prim[NF];
+};
+
+// stage state of cell c (materialised planes)
+__device__ __forceinline__ void uload(const double *S, long long n, long long c, double *u)
+{
+#pragma unroll
+    for (int k = 0; k < NF; ++k) u[k] = __ldg(S + k * n + c);
+}
+
+template <class A>
+__device__ __forceinline__ double usplit(const double *cl, const double *cr, const double *nrm, double *F)
+{
+    if (IsExact<A>::value) {
+        // euler.cpp:42-73
+        double pl[NF], pr[NF], fl[NF], fr[NF];
+        ExactArith::cons2prim(cl, pl);
+        ExactArith::cons2prim(cr, pr);
+        ExactArith::eval_fluxes(cl, pl, nrm, fl);
+        ExactArith::eval_fluxes(cr, pr, nrm, fr);
+        const double lamL = fabs(ExactArith::normal_velocity(pl, nrm)) + sqrt(GAMMA * pl[4]);
+        const double lamR = fabs(ExactArith::normal_velocity(pr, nrm)) + sqrt(GAMMA * pr[4]);
+        return ExactArith::face(cl, fl, lamL, cr, fr, lamR, F);
+    } else {
+        // fast: one reciprocal and one square root per side, flux along n
+        double f[2][NF], lam[2];
+        const double *cs[2] = {cl, cr};
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const double *c = cs[s];
+            const double ri = rcp_newton(c[0]);
+            const double u = c[1] * ri, v = c[2] * ri, w = c[3] * ri;
+            const double p = (GAMMA - 1.0) * fma(-0.5, fma(c[3], w, fma(c[2], v, c[1] * u)), c[4]);
+            const double a = sqrt_newton(GAMMA * p * ri);
+            const double un = fma(w, nrm[2], fma(v, nrm[1], u * nrm[0]));
+            const double mn = c[0] * un;
+            f[s][0] = mn;
+            f[s][1] = fma(mn, u, p * nrm[0]);
+            f[s][2] = fma(mn, v, p * nrm[1]);
+            f[s][3] = fma(mn, w, p * nrm[2]);
+            f[s][4] = un * (c[4] + p);
+            lam[s] = fabs(un) + a;
+        }
+        const double lambda = max_nonneg(lam[0], lam[1]);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) F[k] = 0.5 * fma(-lambda, cr[k] - cl[k], f[0][k] + f[1][k]);
+        return lambda;
+    }
+}
+
+template <class A, int STAGE>
+__global__ void __launch_bounds__(256) uface_kernel(UMesh m, const double *state, double *P, Ctrl *ctrl,
+                                                    double *rhs_maxeig)
+{
+    if (STAGE != STAGE_RHS) {
+        const bool active = (STAGE == STAGE_1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps)
+                                               : ctrl->active != 0;
+        if (!active) return;
+    }
+    const long long n = m.ncells, nf = m.nfaces;
+    double lmax = 0.0;
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
+        const long long o = m.owner[f], nb = m.neigh[f];
+        const bool os = m.solved[o] != 0;
+        const bool ns = nb >= 0 && m.solved[nb] != 0;
+        double F[NF] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (os || ns) {
+            const double nrm[3] = {__ldg(m.normal + f), __ldg(m.normal + nf + f), __ldg(m.normal + 2 * nf + f)};
+            double co[NF], cn[NF];
+            const int bc = m.bc[f];
+            if (bc == BC_NONE) {
+                uload(state, n, o, co);
+                uload(state, n, nb, cn);
+            } else {
+                double n2[3] = {nrm[0], nrm[1], nrm[2]};
+                double *fluid = os ? co : cn, *virt = os ? cn : co;
+                if (!os) { n2[0] = -1. * n2[0]; n2[1] = -1. * n2[1]; n2[2] = -1. * n2[2]; }
+                uload(state, n, os ? o : nb, fluid);
+                ghost_state<ExactArith>(bc, n2, fluid, m.dir_prim, virt);
+            }
+            const double lam = usplit<A>(co, cn, nrm, F);
+            lmax = max_nonneg(lmax, lam);
+            const double ar = __ldg(m.area + f);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) F[k] = ar * F[k];
+        }
+#pragma unroll
+        for (int k = 0; k < NF; ++k) P[k * nf + f] = F[k];
+    }
+    if (STAGE <= STAGE_1) {
+        lmax = warp_max(lmax);
+        if ((threadIdx.x & 31) == 0) {
+            unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)rhs_maxeig : &ctrl->maxeig_bits;
+            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        }
+    }
+}
+
+// Residual gather + stage combination (state = this stage's input, out = its output).
+template <class A, int STAGE>
+__global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, const double *U, const double *state,
+                                                    double *out, Ctrl *ctrl)
+{
+    StepScalars sc;
+    sc.dt = 0.0;
+    sc.s = 0.0;
+    sc.active = true;
+    if (STAGE != STAGE_RHS) {
+        if (STAGE == STAGE_1) {
+            sc.active = (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps);
+            if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->active = sc.active ? 1 : 0;
+        } else {
+            sc.active = ctrl->active != 0;
+            sc.dt = ctrl->dt;
+        }
+        if (STAGE == STAGE_3 && sc.active && blockIdx.x == 0 && threadIdx.x == 0) {
+            ctrl->last_maxeig = __longlong_as_double((long long)ctrl->maxeig_bits);
+            ctrl->t += sc.dt;
+            ctrl->step += 1;
+            ctrl->maxeig_bits = 0ull;
+        }
+        if (!sc.active) return;
+    }
+    const long long n = m.ncells, nf = m.nfaces;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        double acc[NF] = {0., 0., 0., 0., 0.};
+        const bool solved = m.solved[c] != 0;
+        if (solved) {
+            const long long e = m.csr_off[c + 1];
+            for (long long i = m.csr_off[c]; i < e; ++i) {
+                const long long code = m.csr_face[i];
+                const bool owner = code < 0;
+                const long long f = owner ? -code - 1 : code;
+#pragma unroll
+                for (int k = 0; k < NF; ++k) {
+                    const double p = __ldg(P + k * nf + f);
+                    acc[k] = owner ? acc[k] - p : acc[k] + p;    // euler.cpp:237-247
+                }
+            }
+        }
+        const double V = m.vol[c];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            const long long o = k * n + c;
+            if (STAGE == STAGE_RHS || STAGE == STAGE_1) {
+                out[o] = acc[k];
+            } else if (!solved) {
+                continue;                          // unsolved cells keep their state (main.cpp:411-414)
+            } else if (STAGE == STAGE_2) {
+                const double u = __ldg(U + o), w = __ldg(state + o);
+                out[o] = IsExact<A>::value ? 0.75 * u + 0.25 * (w + sc.dt * acc[k] / V)
+                                           : fma(0.25, fma(sc.dt / V, acc[k], w), 0.75 * u);
+            } else {
+                const double u = U[o], w = __ldg(state + o);
+                out[o] = IsExact<A>::value ? (1. / 3) * u + (2. / 3) * (w + sc.dt * acc[k] / V)
+                                           : fma(2.0 / 3.0, fma(sc.dt / V, acc[k], w), u * (1.0 / 3.0));
+            }
+        }
+    }
+}
+
+// W1 = U + dt R1 / V for solved cells, with the dt of main.cpp:398-402.
+template <class A>
+__global__ void __launch_bounds__(256) uform_w1_kernel(UMesh m, const double *U, const double *R, double *W, Ctrl *ctrl)
+{
+    const bool active = ctrl->active != 0;
+    if (!active) return;
+    const double maxEig = __longlong_as_double((long long)ctrl->maxeig_bits);
+    double dt = ctrl->cfl_h / maxEig;
+    if (ctrl->t + dt > ctrl->t_end) dt = ctrl->t_end - ctrl->t;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->dt = dt;
+    const long long n = m.ncells;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < NF * n; i += (long long)gridDim.x * blockDim.x) {
+        const long long c = i % n;
+        if (!m.solved[c]) continue;
+        const double u = __ldg(U + i), r = __ldg(R + i), V = m.vol[c];
+        W[i] = IsExact<A>::value ? u + dt * r / V : fma(dt / V, r, u);
+    }
+}
+
+} // namespace mmf

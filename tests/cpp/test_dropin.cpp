@@ -6,7 +6,10 @@
  * (test infrastructure); a small MeshGeometricalInfo-like class provides the
  * accessors the adapter reads.  Initial states come from the C oracle.
  *
- * usage: test_dropin <radsod|vortex_xy> <dim> <nCells> <steps> <out_loop.bin> <out_stepper.bin>
+ * usage: test_dropin <radsod|vortex_xy> <dim> <nCells> <steps> <out_loop.bin> <out_stepper.bin> [body]
+ * 'body' makes the cells whose centroid lies in [1, 2.5] x [-1.5, 1.5] (x
+ * [-10, 10]) solid and their fluid faces walls (main.cpp:222-277); the
+ * adapter then runs on the face-list kernels.
  */
 #include "bitpit_voloctree.hpp"
 #include "minimmerflow_gb300.hpp"
@@ -36,6 +39,7 @@ public:
         for (std::size_t r = 0; r < patch.getInterfaces().size(); ++r) {
             m_interfaces.push_back(r);
             m_normals.push_back(patch.evalInterfaceNormal((long)r));
+            m_areas.push_back(patch.evalInterfaceArea((long)r));
         }
     }
     int getDimension() const { return m_patch.getDimension(); }
@@ -46,12 +50,13 @@ public:
     double rawGetCellSize(std::size_t r) const { return m_sizes[r]; }
     double rawGetCellVolume(std::size_t r) const { return m_volumes[r]; }
     const std::array<double, 3> &rawGetInterfaceNormal(std::size_t r) const { return m_normals[r]; }
+    double rawGetInterfaceArea(std::size_t r) const { return m_areas[r]; }
 
 private:
     const VolumeKernel &m_patch;
     std::vector<std::size_t> m_cells, m_interfaces;
     std::vector<std::array<double, 3>> m_centroids, m_normals;
-    std::vector<double> m_sizes, m_volumes;
+    std::vector<double> m_sizes, m_volumes, m_areas;
 };
 
 int main(int argc, char **argv)
@@ -72,10 +77,17 @@ int main(int argc, char **argv)
     CellStorageBool solved(1, &mesh.getCells());
     CellStorageDouble U(5, &mesh.getCells()), W(5, &mesh.getCells()), RHS(5, &mesh.getCells());
     InterfaceStorageInt bcs(1, &mesh.getInterfaces());
-    for (std::size_t r = 0; r < nCells; ++r) solved.rawSet(r, true);
-    for (std::size_t f : meshInfo.getInterfaceRawIds())
-        bcs[(long)f] = mesh.getInterfaces().rawAt(f).isBorder()
-                           ? (problem == ORC_RADSOD ? MMF_BC_REFLECTING : MMF_BC_FREE_FLOW) : MMF_BC_NONE;
+    const bool body = argc > 7 && std::strcmp(argv[7], "body") == 0;
+    for (std::size_t r = 0; r < nCells; ++r) {
+        const std::array<double, 3> &c = meshInfo.rawGetCellCentroid(r);
+        const bool solid = body && c[0] > 1.0 && c[0] < 2.5 && c[1] > -1.5 && c[1] < 1.5;
+        solved.rawSet(r, !solid);
+    }
+    for (std::size_t f : meshInfo.getInterfaceRawIds()) {
+        const Interface &itf = mesh.getInterfaces().rawAt(f);
+        if (itf.isBorder()) bcs[(long)f] = (problem == ORC_RADSOD ? MMF_BC_REFLECTING : MMF_BC_FREE_FLOW);
+        else bcs[(long)f] = (solved.rawAt(itf.getOwner()) != solved.rawAt(itf.getNeigh())) ? MMF_BC_WALL : MMF_BC_NONE;
+    }
     orc_params prm;
     orc_params_default(&prm);
     for (std::size_t r = 0; r < nCells; ++r)
@@ -89,22 +101,37 @@ int main(int argc, char **argv)
         mmf_gb300::reconstruction::computePolynomials(problem, meshInfo, solved, U, bcs);
         mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, U, bcs, &RHS, &maxEig);
         double dt = 0.9 * cfl * minCellSize / maxEig;
-        for (std::size_t r = 0; r < nCells; ++r)
+        for (std::size_t r = 0; r < nCells; ++r) {
+            if (!solved.rawAt(r)) continue;
             for (int k = 0; k < 5; ++k) W.rawData(r)[k] = U.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r);
+        }
         mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, W, bcs, &RHS, &maxEig);
-        for (std::size_t r = 0; r < nCells; ++r)
+        for (std::size_t r = 0; r < nCells; ++r) {
+            if (!solved.rawAt(r)) continue;
             for (int k = 0; k < 5; ++k)
                 W.rawData(r)[k] = 0.75 * U.rawData(r)[k] + 0.25 * (W.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r));
+        }
         mmf_gb300::euler::computeRHS(problem, meshInfo, solved, 1, W, bcs, &RHS, &maxEig);
-        for (std::size_t r = 0; r < nCells; ++r)
+        for (std::size_t r = 0; r < nCells; ++r) {
+            if (!solved.rawAt(r)) continue;
             for (int k = 0; k < 5; ++k)
                 U.rawData(r)[k] = (1. / 3) * U.rawData(r)[k] + (2. / 3) * (W.rawData(r)[k] + dt * RHS.rawData(r)[k] / meshInfo.rawGetCellVolume(r));
+        }
         t += dt;
     }
     FILE *fp = std::fopen(argv[5], "wb");
     std::fwrite(U.rawData(0), sizeof(double), 5 * nCells, fp);
     std::fclose(fp);
 
+    if (body) {
+        // the face-list path has no Stepper in this adapter: write the loop result twice
+        fp = std::fopen(argv[6], "wb");
+        std::fwrite(U.rawData(0), sizeof(double), 5 * nCells, fp);
+        std::fclose(fp);
+        std::printf("steps %d %d t %.17g %.17g\n", steps, steps, t, t);
+        mmf_gb300::releaseContexts(meshInfo);
+        return 0;
+    }
     // the same run kept on the device
     mmf_gb300::Stepper stepper(meshInfo, bcs, MMF_ARITH_REFERENCE);
     stepper.upload(U0);
@@ -116,6 +143,6 @@ int main(int argc, char **argv)
     std::fwrite(U0.rawData(0), sizeof(double), 5 * nCells, fp);
     std::fclose(fp);
     std::printf("steps %d %lld t %.17g %.17g\n", steps, (long long)done, t, t2);
-    mmf_gb300::releaseContext(meshInfo);
+    mmf_gb300::releaseContexts(meshInfo);
     return (done == steps && t == t2) ? 0 : 1;
 }

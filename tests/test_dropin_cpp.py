@@ -31,15 +31,20 @@ def test_dropin_builds(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("problem,dim,n,steps", [("radsod", 2, 64, 12), ("vortex_xy", 3, 16, 6)])
-def test_dropin_loop_matches_oracle(orc, tmp_path, problem, dim, n, steps):
+@pytest.mark.parametrize("problem,dim,n,steps,body", [("radsod", 2, 64, 12, False), ("vortex_xy", 3, 16, 6, False),
+                                                      ("vortex_xy", 2, 64, 20, True)])
+def test_dropin_loop_matches_oracle(orc, tmp_path, problem, dim, n, steps, body):
     exe = build_dropin(tmp_path)
     a, b = str(tmp_path / "loop.bin"), str(tmp_path / "stepper.bin")
-    out = subprocess.check_output([exe, problem, str(dim), str(n), str(steps), a, b], timeout=300).decode()
+    cmd = [exe, problem, str(dim), str(n), str(steps), a, b] + (["body"] if body else [])
+    out = subprocess.check_output(cmd, timeout=300).decode()
     assert out.startswith("steps")
     prob = orc.PROBLEMS[problem]
     origin, length = orc.reference_domain(prob)
     m = orc.OracleMesh(prob, dim, (n, n, n if dim == 3 else 1), origin, length)
+    if body:
+        from test_gpu_umesh import with_body
+        with_body(orc, m, ((1.0, -1.5, -10), (2.5, 1.5, 10)))
     U_ref, t, s = m.run(m.initial_state(), 0.45, max_steps=steps)
     assert np.array_equal(np.fromfile(a).reshape(-1, 5), U_ref)
     assert np.array_equal(np.fromfile(b).reshape(-1, 5), U_ref)
