@@ -258,11 +258,11 @@ namespace reconstruction {
 /* reconstruction::computePolynomials (src/reconstruction.cpp:47-55): order 1
  * needs no polynomial data. */
 template <class ProblemType, class MeshInfo, class CellStorageBool, class CellStorageDouble, class InterfaceStorageInt>
-void computePolynomials(ProblemType, const MeshInfo &meshInfo, const CellStorageBool &, const CellStorageDouble &,
-                        const InterfaceStorageInt &interfaceBCs)
+void computePolynomials(ProblemType, const MeshInfo &, const CellStorageBool &, const CellStorageDouble &,
+                        const InterfaceStorageInt &)
 {
-    Context &ctx = contextFor(meshInfo, interfaceBCs, 1);
-    check(mmf_compute_polynomials(ctx.get(), nullptr, nullptr, nullptr, ctx.nCells()));
+    // order 1: nothing to compute, and no context is created here (the first
+    // computeRHS call chooses the Cartesian or the face-list kernels)
 }
 }
 
