@@ -132,6 +132,18 @@ def dist_setup(args):
     return world, rank, local, dist
 
 
+def replica_throughput(total_seconds, units_per_rank, world, dist):
+    """Replicas: every rank runs the same workload on its own GPU with no data
+    exchange; the job time is the slowest rank's, and the job processed
+    world x units_per_rank cell-updates.  Returns (value, job seconds)."""
+    if dist is not None:
+        import torch
+        tt = torch.tensor([float(total_seconds)], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_seconds = float(tt.item())
+    return world * units_per_rank / total_seconds, total_seconds
+
+
 # ---------------------------------------------------------------- CPU baseline
 def cpu_sample_worker(args):
     """One process: oracle steps of the workload, bounded by wall time."""
@@ -223,12 +235,7 @@ def run_batched(args, world, rank, local, dist):
         durs.append(e0.elapsed_time(e1) / 1e3)
     clocks = clk.stop()
     launches = b.launch_count - launches0
-    total = sum(durs)
-    if dist is not None:
-        tt = torch.tensor([total], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total = float(tt.item())
-    value = world * b.total * args.steps / total
+    value, total = replica_throughput(sum(durs), b.total * args.steps, world, dist)
     status_bad = sum(1 for i in range(len(cases)) if b.case_info(i)[2])
     # accuracy: the vortex cases after 'acc_steps' steps against the exact solution
     acc = None
@@ -306,6 +313,9 @@ def run_learned(args, world, rank, local, dist):
         s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
         s.advance(args.warmup)
         launches0 = s.launch_count
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
         durs = []
         for _ in range(args.steps):
             flush.zero_()
@@ -317,7 +327,8 @@ def run_learned(args, world, rank, local, dist):
             e1.record(stream)
             e1.synchronize()
             durs.append(e0.elapsed_time(e1) / 1e3)
-        out[mode] = dict(value=case.ncells * args.steps / sum(durs), ms=1e3 * sum(durs) / args.steps,
+        value, total = replica_throughput(sum(durs), case.ncells * args.steps, world, dist)
+        out[mode] = dict(value=value, ms=1e3 * total / args.steps,
                          launches=s.launch_count - launches0, status=s.status())
         finals[mode] = s.download()
         if mode == "learned":
@@ -368,8 +379,14 @@ def workload_config(args, world):
                              "rho-ratio U[2,10] (transmissive [-1,1]^2), CFL 0.5 per case, order 1, FP64"
                              % (args.ncases, args.seed)),
                 "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
+    if args.workload == "facelist":
+        return {"workload": ("2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, order 1, FP64, through the face-list "
+                             "solver (the mesh given as MeshGeometricalInfo-like face arrays)" % (args.n, args.n)),
+                "cells": args.n * args.n, "l2": "state and face arrays larger than L2",
+                "parallelism": "replicas x%d" % world}
     if args.workload == "sod2d":
-        w = "2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL 0.5, to t=0.25, order 1, FP64" % (args.n, args.n)
+        w = ("2D radial Sod %dx%d, [-1,1]^2, r<0.5, CFL %s, to t=0.25, order %d, FP64"
+             % (args.n, args.n, "0.5" if args.order == 1 else "%.2f" % args.cfl_order2, args.order))
         cells = args.n * args.n
     else:
         w = ("3D isentropic vortex %d^3, [-5,5]^3, periodic, beta=5, axis %s, CFL 0.5, 50-step runs, order 1, FP64"
@@ -377,6 +394,35 @@ def workload_config(args, world):
         cells = args.n ** 3
     return {"workload": w, "cells": cells, "l2": "flushed between timed steps (512 MB write)",
             "parallelism": "replicas x%d" % world}
+
+
+def run_facelist(args, world, rank, local, dist):
+    """The 2D Sod through the face-list solver: one thread per face, then one
+    per cell gathering its faces (CSR, reference order).  K steps timed with a
+    device synchronisation on both sides (the face-list context replays its
+    steps from a CUDA graph inside mmf_umesh_advance)."""
+    import torch
+    import minimmerflow_gb300 as mmf
+    from minimmerflow_gb300.umesh import UnstructuredEuler
+
+    torch.cuda.set_device(local)
+    case = mmf.problem.radial_sod_2d(n=args.n)
+    u = UnstructuredEuler.cartesian(case, arith=args.arith, device=local)
+    u.upload(case.initial_state())
+    u.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
+    u.advance(args.warmup)
+    launches0 = u.launch_count
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u.advance(args.steps)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    value, total = replica_throughput(secs, case.ncells * args.steps, world, dist)
+    launches = u.launch_count - launches0
+    u.close()
+    return dict(value=value, total=total, launches=launches, ncell=case.ncells)
 
 
 def run_ours(args, world, rank, local, dist):
@@ -439,12 +485,7 @@ def run_ours(args, world, rank, local, dist):
     torch.cuda.synchronize()
     clocks = clk.stop()
     launches = s.launch_count - launches0
-    total = sum(durs)
-    if dist is not None:
-        tt = torch.tensor([total], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total = float(tt.item())
-    value = world * ncell * args.steps / total
+    value, total = replica_throughput(sum(durs), ncell * args.steps, world, dist)
 
     # per-stage launch times (the dominant stage kernel gives the roofline)
     stage_t = {1: [], 2: [], 3: []}
@@ -491,7 +532,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
     ap.add_argument("--workload", default="sod2d",
-                    choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned"])
+                    choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned", "facelist"])
     ap.add_argument("--threshold", type=float, default=0.0, help="0 = the calibrated threshold of the weights file")
     ap.add_argument("--learned", action="store_true")
     ap.add_argument("--cfl-order2", type=float, default=0.4)
@@ -527,6 +568,17 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.workload == "facelist":
+        r = run_facelist(args, world, rank, local, dist)
+        if rank != 0:
+            return
+        line = {"metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(args, world), "arith": args.arith, "gpu_launches": r["launches"],
+                "timing": "host clock around a synchronised K-step advance"}
+        print(json.dumps(line))
+        return
     if args.workload == "sod3d_learned":
         r = run_learned(args, world, rank, local, dist)
         if rank != 0:

@@ -157,6 +157,41 @@ int mmf_eval_splitting(int64_t n, const double *cons_l, const double *cons_r, co
 int mmf_eval_bc_values(int64_t n, int bc_type, const double *normal, const double *cons,
                        const double *dirichlet_prim, double *cons_bc);
 
+/* ---- initial states, errors, output, checkpoints ------------------------ */
+/* Problem types (src/problem.hpp:33-42) and the parameters the reference
+ * hard-codes (vortex strength 5, Sod radius 1 and states 1/1 inside,
+ * 0.125/0.1 outside; src/problem.cpp:257-262, 336-342). */
+#define MMF_VORTEX_XY 0
+#define MMF_VORTEX_ZX 1
+#define MMF_VORTEX_YZ 2
+#define MMF_RADSOD 3
+#define MMF_SOD_X 4
+#define MMF_SOD_Y 5
+#define MMF_SOD_Z 6
+#define MMF_FFSTEP 7
+typedef struct {
+    int problem;
+    double vortex_beta;
+    double sod_radius, sod_rho_in, sod_p_in, sod_rho_out, sod_p_out;
+    int periodic_exact;   /* translated vortex wrapped into the domain (periodic borders) */
+} mmf_problem;
+/* Initial conservative state at every cell centroid, on the device
+ * (src/main.cpp:335-344 with src/problem.cpp:247-392). */
+int mmf_init_state(mmf_ctx *ctx, const mmf_problem *problem);
+/* sum over cells of |rho - rho_exact(t)| V on the device (src/main.cpp:550-567). */
+int mmf_l1_density_error(mmf_ctx *ctx, const mmf_problem *problem, double t, double *error);
+/* VTK XML ImageData file (raw appended data, grid order) with the cell
+ * fields of the reference's writer (src/main.cpp:289-298,
+ * src/solver_writer.cpp:56-119): solved, velocity, pressure, temperature,
+ * density and residualC/MX/MY/MZ/E.  The residuals are computeRHS of the
+ * written state with the reference arithmetic (the reference writes the
+ * residual of its last stage's input, which the fused step does not keep). */
+int mmf_write_vtk(mmf_ctx *ctx, const char *path);
+/* Raw checkpoint of the state and the time control (t, step, dt, ...) and
+ * its restore; mmf_advance continues the run where it stopped. */
+int mmf_save_checkpoint(mmf_ctx *ctx, const char *path);
+int mmf_load_checkpoint(mmf_ctx *ctx, const char *path);
+
 /* ---- general face lists ------------------------------------------------ */
 /* The Euler step on any mesh given as MeshGeometricalInfo-like arrays
  * (src/mesh_info.hpp:31-105): per raw cell volume, size and solved flag

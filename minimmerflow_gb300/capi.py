@@ -31,6 +31,7 @@ EXPORTS = [
     "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
     "mmf_umesh_create", "mmf_umesh_destroy", "mmf_umesh_launch_count", "mmf_umesh_upload", "mmf_umesh_download",
     "mmf_umesh_compute_rhs", "mmf_umesh_time_setup", "mmf_umesh_advance",
+    "mmf_init_state", "mmf_l1_density_error", "mmf_write_vtk", "mmf_save_checkpoint", "mmf_load_checkpoint",
 ]
 LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
@@ -47,6 +48,12 @@ class UMeshDesc(C.Structure):
                 ("cell_volume", C.c_void_p), ("cell_size", C.c_void_p), ("solved", C.c_void_p),
                 ("owner", C.c_void_p), ("neigh", C.c_void_p), ("area", C.c_void_p), ("normal", C.c_void_p),
                 ("bc", C.c_void_p), ("dirichlet_prim", C.c_double * 5), ("arith", C.c_int)]
+
+
+class Problem(C.Structure):
+    _fields_ = [("problem", C.c_int), ("vortex_beta", C.c_double), ("sod_radius", C.c_double),
+                ("sod_rho_in", C.c_double), ("sod_p_in", C.c_double), ("sod_rho_out", C.c_double),
+                ("sod_p_out", C.c_double), ("periodic_exact", C.c_int)]
 
 
 class MMFError(RuntimeError):
@@ -142,6 +149,11 @@ def load(build_if_missing=True):
     L.mmf_umesh_compute_rhs.argtypes = [_P, _P, _P, _D, C.c_int64]
     L.mmf_umesh_time_setup.argtypes = [_P, C.c_double, C.c_double, C.c_double, C.c_int64]
     L.mmf_umesh_advance.argtypes = [_P, C.c_int64, _D, C.POINTER(C.c_int64)]
+    L.mmf_init_state.argtypes = [_P, C.POINTER(Problem)]
+    L.mmf_l1_density_error.argtypes = [_P, C.POINTER(Problem), C.c_double, _D]
+    L.mmf_write_vtk.argtypes = [_P, C.c_char_p]
+    L.mmf_save_checkpoint.argtypes = [_P, C.c_char_p]
+    L.mmf_load_checkpoint.argtypes = [_P, C.c_char_p]
     L.mmf_compute_rhs_noalloc.argtypes = [C.POINTER(Grid), _P, _P, _P, _P, _P]
     _lib = L
     return L

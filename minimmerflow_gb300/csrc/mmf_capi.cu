@@ -79,80 +79,7 @@ int mlp_dim(const mmf_mlp *p);
 int mlp_error(mmf_mlp *p);
 }
 
-struct mmf_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    mmf_grid grid;
-    GridParams gp;
-    double *U = nullptr, *R = nullptr, *W = nullptr;   // SoA [5][plane]
-    double *S = nullptr;                               // scratch state (compute_rhs)
-    double *aos = nullptr;                             // AoS staging [plane][5]
-    long long *raw_to_cell = nullptr;                  // null = identity
-    Ctrl *ctrl = nullptr;
-    double *rhs_maxeig = nullptr;
-    cudaGraphExec_t graph_many = nullptr, graph_one = nullptr;
-    long long launches = 0;
-    double cfl = 0.0;
-    bool time_ready = false;
-    bool w_zero = false;      // 2D state with identically zero z-momentum
-    int *flag = nullptr;      // device scratch flag
-    // order 2
-    double *Sl = nullptr;               // slopes, dim x 5 planes
-    unsigned char *lim_flag = nullptr;  // per cell: limit (1) / central slope (0) in LIMIT_FLAGGED mode
-    unsigned char *lim_active = nullptr;// per cell: the limiter changed a slope (stage 1 of the last step)
-    int limit_mode = LIMIT_ALL;
-    mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
-    float ind_threshold = 0.5f;
-
-    cudaError_t stage(int st, const double *U_in, double *out)
-    {
-        StageArgs sa;
-        sa.U = U_in;
-        sa.R = R;
-        sa.W = W;
-        sa.out = out;
-        sa.ctrl = ctrl;
-        sa.rhs_maxeig = rhs_maxeig;
-        ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_stage_fast(st, gp, sa, stream, w_zero)
-                                                                : launch_stage_exact(st, gp, sa, stream);
-    }
-    cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
-    {
-        StageArgs sa;
-        sa.U = U; sa.R = R; sa.W = W; sa.out = out; sa.ctrl = ctrl; sa.rhs_maxeig = rhs_maxeig;
-        O2Args oa;
-        oa.state = state; oa.S = Sl; oa.flag = lim_flag; oa.active = active; oa.limit_mode = limit_mode;
-        oa.ctrl = ctrl; oa.stage = st;
-        ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? launch_o2_fast(op, st, gp, sa, oa, W, stream, w_zero)
-                                                                : launch_o2_exact(op, st, gp, sa, oa, W, stream);
-    }
-    cudaError_t rk_step()
-    {
-        cudaError_t e;
-        if (grid.order == 2) {
-            // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
-            // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
-            if (indicator) {
-                ++launches;
-                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream)) != cudaSuccess)
-                    return e;
-            }
-            if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
-            if ((e = o2(O2_STAGE, STAGE_1, U, R, nullptr)) != cudaSuccess) return e;
-            if ((e = o2(O2_FORM_W1, STAGE_2, U, W, nullptr)) != cudaSuccess) return e;
-            if ((e = o2(O2_SLOPES, STAGE_2, W, nullptr, nullptr)) != cudaSuccess) return e;
-            if ((e = o2(O2_STAGE, STAGE_2, W, R, nullptr)) != cudaSuccess) return e;
-            if ((e = o2(O2_SLOPES, STAGE_3, R, nullptr, nullptr)) != cudaSuccess) return e;
-            return o2(O2_STAGE, STAGE_3, R, U, nullptr);
-        }
-        if ((e = stage(STAGE_1, U, R)) != cudaSuccess) return e;
-        if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
-        return stage(STAGE_3, U, U);
-    }
-    int launches_per_step() const { return grid.order == 2 ? (indicator ? 8 : 7) : 3; }
-};
+#include "mmf_context.cuh"
 
 static int check_ctx(mmf_ctx *ctx)
 {
@@ -290,7 +217,7 @@ static int to_soa(mmf_ctx *c, const double *d_aos, double *soa, int64_t n_raw)
 
 // After a state upload: choose the 2D kernels without z-momentum when that
 // plane is identically zero (the graphs are rebuilt when the choice changes).
-static int refresh_w_zero(mmf_ctx *c)
+static int refresh_w_zero_impl(mmf_ctx *c)
 {
     bool wz = false;
     if (c->gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST) {
@@ -329,7 +256,7 @@ int mmf_upload_state(mmf_ctx *c, const double *aos, int64_t n_raw)
     if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
     MMF_CUDA(cudaMemcpyAsync(c->aos, aos, sizeof(double) * NF * n_raw, cudaMemcpyHostToDevice, c->stream));
     if ((rc = to_soa(c, c->aos, c->U, n_raw))) return rc;
-    return refresh_w_zero(c);
+    return refresh_w_zero_impl(c);
 }
 
 int mmf_download_state(mmf_ctx *c, double *aos, int64_t n_raw)
@@ -349,7 +276,7 @@ int mmf_upload_state_device(mmf_ctx *c, const double *d_aos, int64_t n_raw)
     if (rc) return rc;
     if (!d_aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
     if ((rc = to_soa(c, d_aos, c->U, n_raw))) return rc;
-    return refresh_w_zero(c);
+    return refresh_w_zero_impl(c);
 }
 
 int mmf_download_state_device(mmf_ctx *c, double *d_aos, int64_t n_raw)
@@ -856,3 +783,5 @@ int mmf_newton_selftest(int64_t n, const double *x, double *rcp, double *sqrt_ou
 }
 
 } // extern "C"
+
+int mmf::refresh_w_zero(mmf_ctx *c) { return refresh_w_zero_impl(c); }

@@ -1,0 +1,97 @@
+// mmf_context.cuh -- the solver context of the C ABI (private to the library's
+// translation units).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/mmf_gb300.h"
+#include "mmf_launch.cuh"
+
+namespace mmf {
+cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
+                          unsigned char *flags, cudaStream_t s);
+}
+
+using namespace mmf;
+
+struct mmf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    mmf_grid grid;
+    GridParams gp;
+    double *U = nullptr, *R = nullptr, *W = nullptr;   // SoA [5][plane]
+    double *S = nullptr;                               // scratch state (compute_rhs)
+    double *aos = nullptr;                             // AoS staging [plane][5]
+    long long *raw_to_cell = nullptr;                  // null = identity
+    Ctrl *ctrl = nullptr;
+    double *rhs_maxeig = nullptr;
+    cudaGraphExec_t graph_many = nullptr, graph_one = nullptr;
+    long long launches = 0;
+    double cfl = 0.0;
+    bool time_ready = false;
+    bool w_zero = false;      // 2D state with identically zero z-momentum
+    int *flag = nullptr;      // device scratch flag
+    // order 2
+    double *Sl = nullptr;               // slopes, dim x 5 planes
+    unsigned char *lim_flag = nullptr;  // per cell: limit (1) / central slope (0) in LIMIT_FLAGGED mode
+    unsigned char *lim_active = nullptr;// per cell: the limiter changed a slope (stage 1 of the last step)
+    int limit_mode = LIMIT_ALL;
+    mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
+    float ind_threshold = 0.5f;
+
+    cudaError_t stage(int st, const double *U_in, double *out)
+    {
+        StageArgs sa;
+        sa.U = U_in;
+        sa.R = R;
+        sa.W = W;
+        sa.out = out;
+        sa.ctrl = ctrl;
+        sa.rhs_maxeig = rhs_maxeig;
+        ++launches;
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_stage_fast(st, gp, sa, stream, w_zero)
+                                                                : mmf::launch_stage_exact(st, gp, sa, stream);
+    }
+    cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
+    {
+        StageArgs sa;
+        sa.U = U; sa.R = R; sa.W = W; sa.out = out; sa.ctrl = ctrl; sa.rhs_maxeig = rhs_maxeig;
+        O2Args oa;
+        oa.state = state; oa.S = Sl; oa.flag = lim_flag; oa.active = active; oa.limit_mode = limit_mode;
+        oa.ctrl = ctrl; oa.stage = st;
+        ++launches;
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_o2_fast(op, st, gp, sa, oa, W, stream, w_zero)
+                                                                : mmf::launch_o2_exact(op, st, gp, sa, oa, W, stream);
+    }
+    cudaError_t rk_step()
+    {
+        cudaError_t e;
+        if (grid.order == 2) {
+            // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
+            // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
+            if (indicator) {
+                ++launches;
+                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream)) != cudaSuccess)
+                    return e;
+            }
+            if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
+            if ((e = o2(O2_STAGE, STAGE_1, U, R, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_FORM_W1, STAGE_2, U, W, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_SLOPES, STAGE_2, W, nullptr, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_STAGE, STAGE_2, W, R, nullptr)) != cudaSuccess) return e;
+            if ((e = o2(O2_SLOPES, STAGE_3, R, nullptr, nullptr)) != cudaSuccess) return e;
+            return o2(O2_STAGE, STAGE_3, R, U, nullptr);
+        }
+        if ((e = stage(STAGE_1, U, R)) != cudaSuccess) return e;
+        if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
+        return stage(STAGE_3, U, U);
+    }
+    int launches_per_step() const { return grid.order == 2 ? (indicator ? 8 : 7) : 3; }
+};
+
+
+namespace mmf {
+// After the state changed on the device: pick the 2D kernels without
+// z-momentum when that plane is identically zero (defined in mmf_capi.cu).
+int refresh_w_zero(mmf_ctx *c);
+}

@@ -20,6 +20,16 @@ def _bc(v):
     return _BC_NAMES[v] if isinstance(v, str) else int(v)
 
 
+def problem_struct(case):
+    p = case.prm
+    s = capi.Problem()
+    s.problem = case.problem
+    s.vortex_beta, s.sod_radius = p.vortex_beta, p.sod_radius
+    s.sod_rho_in, s.sod_p_in, s.sod_rho_out, s.sod_p_out = p.sod_rho_in, p.sod_p_in, p.sod_rho_out, p.sod_p_out
+    s.periodic_exact = int(p.periodic)
+    return s
+
+
 class CartesianEuler:
     """Uniform Cartesian FV Euler solver context on one GPU.
 
@@ -183,6 +193,25 @@ class CartesianEuler:
     @property
     def launch_count(self):
         return self._lib.mmf_launch_count(self._ctx)
+
+    def init_state(self, case):
+        """Initial state of a problem case computed on the device (problem.cpp:247-392)."""
+        capi.check(self._lib.mmf_init_state(self._ctx, C.byref(problem_struct(case))))
+
+    def l1_density_error(self, case, t):
+        """sum |rho - rho_exact(t)| V on the device (main.cpp:550-567)."""
+        e = C.c_double()
+        capi.check(self._lib.mmf_l1_density_error(self._ctx, C.byref(problem_struct(case)), t, C.byref(e)))
+        return e.value
+
+    def write_vtk(self, path):
+        capi.check(self._lib.mmf_write_vtk(self._ctx, str(path).encode()))
+
+    def save_checkpoint(self, path):
+        capi.check(self._lib.mmf_save_checkpoint(self._ctx, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        capi.check(self._lib.mmf_load_checkpoint(self._ctx, str(path).encode()))
 
     def run(self, U0, cfl, t_end=math.inf, max_steps=-1, t_start=0.0, batch=1 << 30):
         """Reference loop (main.cpp:377-506) from U0 to t_end / max_steps; returns (U, t, steps)."""

@@ -50,6 +50,37 @@ class UnstructuredEuler:
         return cls(m.dim, vol, size, f["owner"], f["neigh"], f["area"], f["normal"], f["bc"], solved=solved,
                    arith=arith, dirichlet_prim=dirichlet_prim)
 
+    @classmethod
+    def cartesian(cls, case, arith="fast", device=0):
+        """The face list of a uniform grid (grid order, x faces then y then z,
+        the border and periodic faces included), as MeshGeometricalInfo would
+        describe it: the normal points from owner to neighbour, a border face
+        has its owner inside (euler.cpp:166-178)."""
+        f = cartesian_faces(case)
+        return cls(case.dim, f["volume"], f["size"], f["owner"], f["neigh"], f["area"], f["normal"], f["bc"],
+                   arith=arith, device=device)
+
+    def upload(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        capi.check(self._lib.mmf_umesh_upload(self._u, capi.ptr(U), self.ncells))
+
+    def download(self):
+        out = np.empty((self.ncells, 5))
+        capi.check(self._lib.mmf_umesh_download(self._u, capi.ptr(out), self.ncells))
+        return out
+
+    def time_setup(self, cfl, t=0.0, t_end=math.inf, max_steps=-1):
+        capi.check(self._lib.mmf_umesh_time_setup(self._u, cfl, t, t_end, max_steps))
+
+    def advance(self, n_steps):
+        tt, done = C.c_double(), C.c_int64()
+        capi.check(self._lib.mmf_umesh_advance(self._u, n_steps, C.byref(tt), C.byref(done)))
+        return tt.value, done.value
+
+    @property
+    def launch_count(self):
+        return int(self._lib.mmf_umesh_launch_count(self._u))
+
     def close(self):
         if getattr(self, "_u", None) is not None and self._u.value:
             self._lib.mmf_umesh_destroy(self._u)
@@ -92,3 +123,43 @@ class UnstructuredEuler:
         out = np.empty((self.ncells, 5))
         capi.check(self._lib.mmf_umesh_download(self._u, capi.ptr(out), self.ncells))
         return out, t, steps
+
+
+def cartesian_faces(case):
+    """Face arrays of the uniform grid of a problem case (see UnstructuredEuler.cartesian)."""
+    dim = case.dim
+    nx, ny, nz = case.n[0], case.n[1], case.n[2] if dim == 3 else 1
+    h = case.h
+    lo, hi = case.bcs()
+    periodic = lo[0] == 16
+    owners, neighs, normals, bcs = [], [], [], []
+    cell = np.arange(nx * ny * nz, dtype=np.int64).reshape(nz, ny, nx)
+    for d in range(dim):
+        c = np.moveaxis(cell, 2 - d, 2)            # direction d last
+        m = c.shape[2]
+        e = np.zeros(3)
+        e[d] = 1.0
+        if periodic:
+            own = np.concatenate([c[:, :, -1:], c[:, :, :-1]], axis=2)
+            nei = c
+            owners.append(own.reshape(-1))
+            neighs.append(nei.reshape(-1))
+            normals.append(np.tile(e, (own.size, 1)))
+            bcs.append(np.full(own.size, -1, dtype=np.int32))
+            continue
+        # faces 0..m along d: 0 and m are borders
+        own = np.concatenate([c[:, :, :1], c[:, :, :-1], c[:, :, -1:]], axis=2)
+        nei = np.concatenate([np.full(c[:, :, :1].shape, -1), c[:, :, 1:], np.full(c[:, :, :1].shape, -1)], axis=2)
+        nrm = np.tile(e, own.shape + (1,))
+        nrm[:, :, 0] = -e
+        b = np.full(own.shape, -1, dtype=np.int32)
+        b[:, :, 0] = lo[d]
+        b[:, :, m] = hi[d]
+        owners.append(own.reshape(-1))
+        neighs.append(nei.reshape(-1))
+        normals.append(nrm.reshape(-1, 3))
+        bcs.append(b.reshape(-1))
+    n = nx * ny * nz
+    return dict(volume=np.full(n, h ** dim), size=np.full(n, h), owner=np.concatenate(owners),
+                neigh=np.concatenate(neighs), area=np.full(sum(o.size for o in owners), h ** (dim - 1)),
+                normal=np.concatenate(normals), bc=np.concatenate(bcs))

@@ -202,6 +202,27 @@ class OracleMesh:
                     centroid=self._arr(self.m.fcentroid, 3 * nf, np.float64).reshape(-1, 3),
                     bc=self._arr(self.m.bc, nf, np.int32), fdir=self._arr(self.m.fdir, nf, np.int32))
 
+    def set_bodies(self, boxes):
+        """Box bodies: a cell is solid when its centroid lies in a box, bounds
+        included (body.cpp:80-95); solid cells are not solved and interior
+        faces between a fluid and a solid cell become BC_WALL
+        (main.cpp:222-277).  boxes = [((xmin, ymin, zmin), (xmax, ymax, zmax)), ...].
+        Returns the solid-cell mask (raw order)."""
+        n, nf = self.ncells, self.nfaces
+        c = self.centroids()
+        solid = np.zeros(n, dtype=bool)
+        for lo, hi in boxes:
+            solid |= np.all((c >= np.asarray(lo, dtype=np.float64)) & (c <= np.asarray(hi, dtype=np.float64)), axis=1)
+        solved = np.ctypeslib.as_array(self.m.solved, shape=(n,))
+        solved[:] = ~solid
+        bc = np.ctypeslib.as_array(self.m.bc, shape=(nf,))
+        owner = np.ctypeslib.as_array(self.m.owner, shape=(nf,))
+        neigh = np.ctypeslib.as_array(self.m.neigh, shape=(nf,))
+        interior = neigh >= 0
+        wall = interior & (solid[owner] != solid[np.where(interior, neigh, 0)])
+        bc[wall] = BC_WALL
+        return solid
+
     def initial_state(self, prm=None):
         prm = prm or params()
         U = np.empty(self.ncells * 5)

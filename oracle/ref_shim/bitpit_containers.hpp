@@ -108,6 +108,7 @@ public:
         return *it->second;
     }
     bool hasSection(const std::string &key) const { return m_sections.count(key) > 0; }
+    const std::map<std::string, std::unique_ptr<Config>> &getSections() const { return m_sections; }
     bool hasOption(const std::string &key) const { return m_options.count(key) > 0; }
     void set(const std::string &key, const std::string &value) { m_options[key] = value; }
     template <typename T>

@@ -7,10 +7,16 @@
  * reconstruction::, euler:: and problem:: functions.
  *
  * usage: mmf_ref <problem> <dim> <nCells> <order> <CFL> <t_end|-|inf> [max_steps] [dump.bin]
+ *               [length=L] [body=xmin,ymin,zmin,xmax,ymax,zmax ...]
  *   '-' takes the problem's default end time (problem.cpp:175-211); 'inf'
- *   runs exactly max_steps steps.
+ *   runs exactly max_steps steps.  length= sets problem.domain.length (the
+ *   forward-facing step has no default); each body= adds a box body to the
+ *   configuration read by the reference's body::initialize (body.cpp:49-72),
+ *   and the fluid / solved flags and the wall faces between fluid and solid
+ *   cells are set up as src/main.cpp:222-277 does.
  * prints "Final error:  %.12e", the step count and the loop time.
  */
+#include "body.hpp"
 #include "constants.hpp"
 #include "euler.hpp"
 #include "mesh_info.hpp"
@@ -41,8 +47,36 @@ int main(int argc, char *argv[])
     const int order = std::atoi(argv[4]);
     const double cfl = std::atof(argv[5]);
     const long nCellsPerDirection = std::atol(argv[3]);
-    const long maxSteps = (argc > 7) ? std::atol(argv[7]) : -1;
-    const char *dump = (argc > 8) ? argv[8] : nullptr;
+    // positional [max_steps] [dump], then key=value options
+    std::vector<const char *> positional;
+    int nBodies = 0;
+    for (int a = 7; a < argc; ++a) {
+        const char *eq = std::strchr(argv[a], '=');
+        if (!eq) { positional.push_back(argv[a]); continue; }
+        const std::string key(argv[a], eq - argv[a]);
+        if (key == "length") {
+            config::root["problem"]["domain"].set("length", eq + 1);
+        } else if (key == "body") {
+            double b[6];
+            if (std::sscanf(eq + 1, "%lf,%lf,%lf,%lf,%lf,%lf", &b[0], &b[1], &b[2], &b[3], &b[4], &b[5]) != 6) {
+                std::fprintf(stderr, "body=xmin,ymin,zmin,xmax,ymax,zmax\n");
+                return 2;
+            }
+            Config &body = config::root["bodies"]["body" + std::to_string(nBodies++)];
+            body.set("type", "box");
+            const char *names[6] = {"xMin", "yMin", "zMin", "xMax", "yMax", "zMax"};
+            for (int k = 0; k < 6; ++k) {
+                char buf[64];
+                std::snprintf(buf, sizeof(buf), "%.17g", b[k]);
+                body.set(names[k], buf);
+            }
+        } else {
+            std::fprintf(stderr, "unknown option %s\n", argv[a]);
+            return 2;
+        }
+    }
+    const long maxSteps = (positional.size() > 0) ? std::atol(positional[0]) : -1;
+    const char *dump = (positional.size() > 1) ? positional[1] : nullptr;
 
     const problem::ProblemType problemType = problem::getProblemType();
     int dimensions;
@@ -66,11 +100,18 @@ int main(int argc, char *argv[])
     const std::vector<std::size_t> &interfaceRawIds = meshInfo.getInterfaceRawIds();
     const std::size_t nInterfaces = interfaceRawIds.size();
 
+    body::initialize();
+
     CellStorageBool cellSolvedFlag(1, &mesh.getCells());
+    CellStorageBool cellFluidFlag(1, &mesh.getCells());
     CellStorageDouble cellConservatives(N_FIELDS, &mesh.getCells());
     CellStorageDouble cellConservativesWork(N_FIELDS, &mesh.getCells());
     CellStorageDouble cellRHS(N_FIELDS, &mesh.getCells());
-    for (std::size_t i = 0; i < nCells; ++i) cellSolvedFlag.rawSet(cellRawIds[i], true);
+    for (std::size_t i = 0; i < nCells; ++i) {
+        const bool isFluid = body::isPointFluid(meshInfo.rawGetCellCentroid(cellRawIds[i]));
+        cellFluidFlag.rawSet(cellRawIds[i], isFluid);
+        cellSolvedFlag.rawSet(cellRawIds[i], isFluid);
+    }
 
     reconstruction::initialize();
 
@@ -78,8 +119,14 @@ int main(int argc, char *argv[])
     for (std::size_t i = 0; i < nInterfaces; ++i) {
         const Interface &interface = mesh.getInterfaces().rawAt(interfaceRawIds[i]);
         long interfaceId = interface.getId();
-        interfaceBCs[interfaceId] = interface.isBorder() ? problem::getBorderBCType(problemType, interfaceId, meshInfo)
-                                                         : BC_NONE;
+        if (interface.isBorder()) {
+            interfaceBCs[interfaceId] = problem::getBorderBCType(problemType, interfaceId, meshInfo);
+        } else {
+            const std::size_t ownerRaw = mesh.getCellConstIterator(interface.getOwner()).getRawIndex();
+            const std::size_t neighRaw = mesh.getCellConstIterator(interface.getNeigh()).getRawIndex();
+            const bool wall = cellFluidFlag.rawAt(ownerRaw) != cellFluidFlag.rawAt(neighRaw);
+            interfaceBCs[interfaceId] = wall ? BC_WALL : BC_NONE;
+        }
     }
 
     for (std::size_t i = 0; i < nCells; ++i) {

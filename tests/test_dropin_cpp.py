@@ -43,8 +43,7 @@ def test_dropin_loop_matches_oracle(orc, tmp_path, problem, dim, n, steps, body)
     origin, length = orc.reference_domain(prob)
     m = orc.OracleMesh(prob, dim, (n, n, n if dim == 3 else 1), origin, length)
     if body:
-        from test_gpu_umesh import with_body
-        with_body(orc, m, ((1.0, -1.5, -10), (2.5, 1.5, 10)))
+        m.set_bodies([((1.0, -1.5, -10), (2.5, 1.5, 10))])
     U_ref, t, s = m.run(m.initial_state(), 0.45, max_steps=steps)
     assert np.array_equal(np.fromfile(a).reshape(-1, 5), U_ref)
     assert np.array_equal(np.fromfile(b).reshape(-1, 5), U_ref)

@@ -12,23 +12,6 @@ from test_gpu_parity import FAST_RTOL, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def with_body(orc, m, box):
-    """Cells whose centroid lies in the box become solid; fluid/solid faces are walls."""
-    n = m.ncells
-    solved = np.ctypeslib.as_array(m.m.solved, shape=(n,))
-    c = m.centroids()
-    inside = np.all((c[:, :m.dim] > np.array(box[0])[:m.dim]) & (c[:, :m.dim] < np.array(box[1])[:m.dim]), axis=1)
-    solved[inside] = 0
-    nf = m.nfaces
-    bc = np.ctypeslib.as_array(m.m.bc, shape=(nf,))
-    owner = np.ctypeslib.as_array(m.m.owner, shape=(nf,))
-    neigh = np.ctypeslib.as_array(m.m.neigh, shape=(nf,))
-    interior = neigh >= 0
-    flip = interior & (solved[owner] != solved[np.where(interior, neigh, 0)])
-    bc[flip] = orc.BC_WALL
-    return inside
-
-
 @pytest.mark.parametrize("name", ["2dIsentropicVortex", "2dRadSod", "3dIsentropicVortexYZ", "3dRadSod"])
 def test_goldens_on_face_lists(orc, mmf, name):
     from minimmerflow_gb300.umesh import UnstructuredEuler
@@ -53,7 +36,7 @@ def test_goldens_on_face_lists(orc, mmf, name):
 def test_immersed_body(orc, mmf, arith):
     from minimmerflow_gb300.umesh import UnstructuredEuler
     m = orc.OracleMesh(orc.VORTEX_XY, 2, (64, 64, 1), (-5, -5, 0), 10.0)
-    inside = with_body(orc, m, ((1.0, -1.5, -10), (2.5, 1.5, 10)))
+    inside = m.set_bodies([((1.0, -1.5, -10), (2.5, 1.5, 10))])
     assert inside.sum() > 50
     U0 = m.initial_state()
     U_ref, t_ref, _ = m.run(U0, 0.45, max_steps=40)
@@ -74,7 +57,7 @@ def test_forward_facing_step(orc, mmf, arith):
     m = orc.OracleMesh(orc.FFSTEP, 2, (64, 64, 1), (0, 0, 0), 3.2)
     bc = m.faces()["bc"]
     assert {orc.BC_DIRICHLET, orc.BC_FREE_FLOW, orc.BC_REFLECTING} <= set(bc.tolist())
-    inside = with_body(orc, m, ((0.6, -1.0, -10), (4.0, 0.2, 10)))
+    inside = m.set_bodies([((0.6, -1.0, -10), (4.0, 0.2, 10))])
     U0 = m.initial_state()
     U_ref, t_ref, _ = m.run(U0, 0.45, max_steps=60)
     dp = [1.0, 3.0, 0.0, 0.0, 1.0 / 1.4]

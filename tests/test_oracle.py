@@ -130,3 +130,31 @@ def test_oracle_matches_reference_build(orc, tmp_path):
         m = orc.golden_mesh(name)
         U, t, steps = m.run(m.initial_state(), cfl, t_end=t_end)
         assert np.array_equal(np.fromfile(dump).reshape(-1, 5), U)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference tree not present")
+@pytest.mark.parametrize("case", ["vortex_body", "ffstep"])
+def test_oracle_bodies_match_reference_build(orc, tmp_path, case):
+    """Immersed box bodies (reference body.cpp, unsolved cells, BC_WALL faces,
+    main.cpp:222-277) and the forward-facing step (problem.cpp:404-477):
+    oracle/_ref and the C restatement give bit-identical final states."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call(["make", "-s", "-f", os.path.join(root, "oracle", "Makefile.ref"),
+                           "REF_SRC=" + REF_SRC], cwd=root, timeout=300)
+    exe = os.path.join(root, "oracle", "_ref", "mmf_ref")
+    dump = str(tmp_path / "final.bin")
+    if case == "vortex_body":
+        box, steps = ((1.0, -1.5, -10.0), (2.5, 1.5, 10.0)), 40
+        args = ["vortex_xy", "2", "64", "1", "0.45", "inf", str(steps), dump]
+        m = orc.OracleMesh(orc.VORTEX_XY, 2, (64, 64, 1), (-5, -5, 0), 10.0)
+    else:
+        box, steps = ((0.6, -1.0, -10.0), (4.0, 0.2, 10.0)), 60
+        args = ["ffstep", "2", "64", "1", "0.45", "inf", str(steps), dump, "length=3.2"]
+        m = orc.OracleMesh(orc.FFSTEP, 2, (64, 64, 1), (0, 0, 0), 3.2)
+    args.append("body=" + ",".join(repr(v) for v in box[0] + box[1]))
+    subprocess.check_output([exe] + args, timeout=300)
+    solid = m.set_bodies([box])
+    assert solid.sum() > 50
+    U, t, s = m.run(m.initial_state(), 0.45, max_steps=steps)
+    assert s == steps
+    assert np.array_equal(np.fromfile(dump).reshape(-1, 5), U)
