@@ -35,6 +35,10 @@ sys.path.insert(0, ROOT)
 
 CELL_BYTES_STEP = 320          # algorithmic HBM bytes per cell-update (8 x 5 fields x 8 B)
 STAGE_BYTES = {1: 80, 2: 120, 3: 120}
+# order 2, per RK stage (slopes + W1 + stage launches), 5 fields x 8 B per plane:
+# 2D slopes read 40 + write 80; 3D slopes read 40 + write 120
+STAGE_BYTES_O2 = {2: {1: 120 + 160, 2: 120 + 120 + 240, 3: 120 + 200},
+                  3: {1: 160 + 200, 2: 120 + 160 + 280, 3: 160 + 240}}
 FP64_OPS_PER_CELL_STAGE = None  # filled from the kernel model below (fast arithmetic, 2D)
 
 
@@ -352,7 +356,10 @@ def run_learned(args, world, rank, local, dist):
 def make_case(args):
     import minimmerflow_gb300 as mmf
     if args.workload == "sod2d":
-        return mmf.problem.radial_sod_2d(n=args.n)
+        case = mmf.problem.radial_sod_2d(n=args.n)
+        if args.order == 2:
+            case.cfl = args.cfl_order2
+        return case
     axis = "z" if args.workload == "vortex3d_z" else "x"
     case = mmf.problem.vortex(3, args.n, axis=axis, steps=50)
     case.t_end = math.inf
@@ -446,6 +453,8 @@ def run_ours(args, world, rank, local, dist):
 
     restart()
     steps_done = 0
+    # decomposition chosen by timing (outside the timed region; the state is restored)
+    tuned = s.autotune(trial_steps=4) if args.chunk <= 0 else (args.chunk, None)
 
     def ensure_room():
         t, st = s.time_info()
@@ -521,7 +530,7 @@ def run_ours(args, world, rank, local, dist):
     e2e_val = world * ncell * k_e2e / e2e_s
     s.close()
     return dict(value=value, total=total, clocks=clocks, launches=launches, st_mean=st_mean, dominant=dominant,
-                e2e=e2e_val, ncell=ncell, case=case)
+                e2e=e2e_val, ncell=ncell, case=case, tuned=tuned)
 
 
 def main():
@@ -628,22 +637,30 @@ def main():
     hbm_peak, peak_src = read_peaks()
     ncell = r["ncell"]
     dom = r["dominant"]
-    achieved = STAGE_BYTES[dom] * ncell / r["st_mean"][dom] / 1e9
+    stage_bytes = STAGE_BYTES if args.order == 1 else STAGE_BYTES_O2[r["case"].dim]
+    achieved = stage_bytes[dom] * ncell / r["st_mean"][dom] / 1e9
     traffic_rec = read_traffic()
     traffic = None
-    if traffic_rec and str(args.n) in traffic_rec.get("per_launch_bytes", {}):
+    if args.order == 1 and traffic_rec and str(args.n) in traffic_rec.get("per_launch_bytes", {}):
         traffic = traffic_rec["per_launch_bytes"][str(args.n)].get("stage%d" % dom)
-    fp64_ops = fp64_ops_per_cell_update_2d() if args.workload == "sod2d" else None
+    fp64_ops = fp64_ops_per_cell_update_2d() if (args.workload == "sod2d" and args.order == 1) else None
+    if r["tuned"][1] is not None:
+        workload = dict(workload, decomposition={"rows_per_chunk" if r["case"].dim == 2 else "planes_per_chunk":
+                                                 r["tuned"][0], "warps_per_block": r["tuned"][1] or None,
+                                                 "chosen_by": "mmf_autotune"})
     fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock)
     line = {
         "metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload,
         "arith": args.arith,
-        "roofline": {"bound": "hbm", "kernel": "stage%d (stage%dd_kernel<%s>)" % (dom, r["case"].dim, args.arith),
+        "roofline": {"bound": "hbm",
+                     "kernel": ("stage%d (stage%dd_kernel<%s>)" % (dom, r["case"].dim, args.arith) if args.order == 1
+                                else "RK stage %d of order 2 (slopes, W1 and stage%dd_o2_kernel launches)"
+                                % (dom, r["case"].dim)),
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": STAGE_BYTES[dom] * ncell,
+                     "algorithmic_bytes_per_launch": stage_bytes[dom] * ncell,
                      "stage_ms": {str(k): 1e3 * v for k, v in r["st_mean"].items()}},
         "fp64": {"ops_per_cell_update_model": fp64_ops,
                  "achieved_ops_per_s": fp64_ops * r["value"] / world if fp64_ops else None,

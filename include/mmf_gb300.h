@@ -132,6 +132,13 @@ int mmf_time_info(mmf_ctx *ctx, double *t, int64_t *step);
 /* The CUDA stream (cudaStream_t) all work of this context is ordered on. */
 void *mmf_get_stream(mmf_ctx *ctx);
 /* Host-buffer form: uploads 'aos', advances n_steps, downloads into 'aos'. */
+/* Chooses the work decomposition of the stage kernels by timing a few steps
+ * of each candidate from the current state (2D: rows per marching chunk x
+ * warps per block; 3D: planes per chunk); restores the state and the time
+ * control afterwards.  Results are bitwise independent of the choice.
+ * Needs mmf_time_setup.  warps_per_block is 0 in 3D.  No reference
+ * counterpart. */
+int mmf_autotune(mmf_ctx *ctx, int trial_steps, int *chunk, int *warps_per_block);
 int mmf_advance_host(mmf_ctx *ctx, double *aos, int64_t n_raw, int64_t n_steps, double *t_out);
 /* Last step's dt and stage-1 maxEig (the reference logs both, main.cpp:399). */
 int mmf_last_step_info(mmf_ctx *ctx, double *dt, double *max_eig);

@@ -3,6 +3,7 @@
 // reference entry points, and the CUDA-graph time loop.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -64,6 +65,33 @@ __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__rest
     if (g < 0 || g >= plane) return;
 #pragma unroll
     for (int k = 0; k < NF; ++k) aos[NF * r + k] = soa[k * plane + g];
+}
+
+// Band [base, base + count) of a state in grid order: AoS -> SoA, and
+// wflag := 1 when a z-momentum value of the band is not +0 / -0.
+__global__ void aos_to_soa_band_kernel(const double *__restrict__ aos, double *__restrict__ soa, long long base,
+                                       long long count, long long plane, int *wflag)
+{
+    bool nz = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long g = base + i;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) soa[k * plane + g] = aos[NF * g + k];
+        nz |= (__double_as_longlong(aos[NF * g + 3]) << 1) != 0;
+    }
+    if (wflag && __any_sync(0xffffffffu, nz) && (threadIdx.x & 31) == 0) atomicOr(wflag, 1);
+}
+
+__global__ void soa_to_aos_band_kernel(const double *__restrict__ soa, double *__restrict__ aos, long long base,
+                                       long long count, long long plane)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long g = base + i;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) aos[NF * g + k] = soa[k * plane + g];
+    }
 }
 
 } // namespace
@@ -177,6 +205,18 @@ int mmf_destroy(mmf_ctx *c)
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
     cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
     cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
+            if (c->ev_up[b]) cudaEventDestroy(c->ev_up[b]);
+            if (c->ev_dn[b]) cudaEventDestroy(c->ev_dn[b]);
+        }
+        if (c->ev_tr) cudaEventDestroy(c->ev_tr);
+        if (c->ev_flag) cudaEventDestroy(c->ev_flag);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    cudaFreeHost(c->h_flag);
+    cudaFreeHost(c->h_ctrl);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MMF_OK;
@@ -610,9 +650,245 @@ int mmf_time_info(mmf_ctx *c, double *t, int64_t *step)
 
 void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+// ---- pipelined host round trip ------------------------------------------
+// The state is cut into K bands along the slowest axis (rows in 2D, planes in
+// 3D).  Band b's upload (copy stream) overlaps the transposition and the
+// stage-1 kernels of the bands already on the device; after stage 2, each
+// band's stage 3 is followed by its transposition and its download (copy
+// stream), which overlaps the stage 3 of the next band.  Stage 2 needs the
+// step's dt, a max over every cell of stage 1, so it runs on the whole grid.
+// Band launches use shorter marching chunks so that each one fills the GPU.
+struct BandPlan {
+    int K = 0;
+    int rows = 0;          // rows (planes) per band, a multiple of chunk
+    int chunk = 0;         // marching chunk of the band launches
+    long long slab = 0;    // cells per row (plane)
+    int n_slow = 0;
+};
+
+static BandPlan band_plan(const mmf_ctx *c)
+{
+    BandPlan p;
+    const GridParams &gp = c->gp;
+    p.n_slow = gp.dim == 2 ? gp.n[1] : gp.n[2];
+    p.slab = gp.dim == 2 ? (long long)gp.n[0] : (long long)gp.n[0] * gp.n[1];
+    if (p.n_slow < 64 || p.slab * p.n_slow < (1 << 18)) return p;   // too small to pay
+    int K = 4;
+    int rows = (p.n_slow + K - 1) / K;
+    int ch;
+    if (gp.dim == 2) ch = (int)std::min<long long>(32, std::max<long long>(4, (long long)gp.nseg * rows / 1216));
+    else ch = (int)std::min<long long>(32, std::max<long long>(2, (long long)gp.nseg * gp.nrowblk * rows / 304));
+    rows = (rows + ch - 1) / ch * ch;
+    p.K = (p.n_slow + rows - 1) / rows;
+    p.rows = rows;
+    p.chunk = ch;
+    return p;
+}
+
+static GridParams band_params(const mmf_ctx *c, const BandPlan &p, int b, int bookkeep)
+{
+    GridParams g = c->gp;
+    const int r0 = b * p.rows, r1 = std::min(p.n_slow, r0 + p.rows);
+    g.chunk = p.chunk;
+    g.chunk0 = r0 / p.chunk;
+    g.nchunk = (r1 - r0 + p.chunk - 1) / p.chunk;
+    g.bookkeep = bookkeep;
+    return g;
+}
+
+static int pipeline_resources(mmf_ctx *c)
+{
+    if (c->copy_stream) return MMF_OK;
+    MMF_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
+        MMF_CUDA(cudaEventCreateWithFlags(&c->ev_up[b], cudaEventDisableTiming));
+        MMF_CUDA(cudaEventCreateWithFlags(&c->ev_dn[b], cudaEventDisableTiming));
+    }
+    MMF_CUDA(cudaEventCreateWithFlags(&c->ev_tr, cudaEventDisableTiming));
+    MMF_CUDA(cudaEventCreateWithFlags(&c->ev_flag, cudaEventDisableTiming));
+    MMF_CUDA(cudaHostAlloc(&c->h_flag, sizeof(int), cudaHostAllocDefault));
+    MMF_CUDA(cudaHostAlloc(&c->h_ctrl, sizeof(Ctrl), cudaHostAllocDefault));
+    return MMF_OK;
+}
+
+static bool pipeline_applies(const mmf_ctx *c, const double *aos, int64_t n_steps)
+{
+    if (c->grid.order != 1 || c->raw_to_cell || n_steps < 1) return false;
+    if (band_plan(c).K < 2 || band_plan(c).K > mmf_ctx::MAX_BANDS) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, aos) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeHost;   // page-locked: the copies run asynchronously
+}
+
+static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, double *t_out)
+{
+    int rc = pipeline_resources(c);
+    if (rc) return rc;
+    const BandPlan p = band_plan(c);
+    const GridParams &gp = c->gp;
+    const long long plane = gp.plane;
+    const bool periodic_slow = (gp.dim == 2 ? gp.bc_lo[1] : gp.bc_lo[2]) == BC_PERIODIC;
+    const bool check_w = gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST;
+    auto band_cells = [&](int b, long long &base, long long &count) {
+        const int r0 = b * p.rows, r1 = std::min(p.n_slow, r0 + p.rows);
+        base = (long long)r0 * p.slab;
+        count = (long long)(r1 - r0) * p.slab;
+    };
+    // band b's stage 1 needs the bands on both sides of it on the device
+    auto need = [&](int b) { return (b == 0 && periodic_slow) ? p.K - 1 : std::min(b + 1, p.K - 1); };
+
+    // upload, transposition and stage 1, band by band
+    MMF_CUDA(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
+    MMF_CUDA(cudaEventRecord(c->ev_tr, c->stream));
+    MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr, 0));   // the device buffers are free
+    for (int b = 0; b < p.K; ++b) {
+        long long base, count;
+        band_cells(b, base, count);
+        MMF_CUDA(cudaMemcpyAsync(c->aos + NF * base, aos + NF * base, sizeof(double) * NF * count,
+                                 cudaMemcpyHostToDevice, c->copy_stream));
+        MMF_CUDA(cudaEventRecord(c->ev_up[b], c->copy_stream));
+    }
+    int launched = 0;   // bands whose stage 1 is enqueued (in order, except band 0 when periodic)
+    std::vector<char> s1((size_t)p.K, 0);
+    for (int b = 0; b < p.K; ++b) {
+        long long base, count;
+        band_cells(b, base, count);
+        MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_up[b], 0));
+        const unsigned blocks = (unsigned)std::min<long long>((count + 255) / 256, 4L * 152);
+        aos_to_soa_band_kernel<<<blocks, 256, 0, c->stream>>>(c->aos, c->U, base, count, plane,
+                                                              check_w ? c->flag : nullptr);
+        ++c->launches;
+        MMF_CUDA(cudaPeekAtLastError());
+        if (b == p.K - 1 && check_w) {
+            MMF_CUDA(cudaEventRecord(c->ev_tr, c->stream));
+            MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr, 0));
+            MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
+            MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
+        }
+        for (int q = 0; q < p.K; ++q)
+            if (!s1[(size_t)q] && need(q) <= b) {
+                MMF_CUDA(c->stage_gp(STAGE_1, band_params(c, p, q, 1), c->U, c->R));
+                s1[(size_t)q] = 1;
+                ++launched;
+            }
+    }
+    if (check_w) {
+        // the stage-1 kernels assumed the previous z-momentum decision; redo
+        // stage 1 on the whole grid if this state does not fit it
+        MMF_CUDA(cudaEventSynchronize(c->ev_flag));
+        const bool wz = (*c->h_flag == 0);
+        if (wz != c->w_zero) {
+            const bool redo = c->w_zero;   // the 4-field kernels skipped a non-zero plane
+            c->w_zero = wz;
+            if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+            if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
+            if (redo) {
+                MMF_CUDA(cudaMemsetAsync(&c->ctrl->maxeig_bits, 0, sizeof(unsigned long long), c->stream));
+                MMF_CUDA(cudaMemsetAsync(&c->ctrl->status, 0, sizeof(unsigned), c->stream));
+                MMF_CUDA(c->stage(STAGE_1, c->U, c->R));
+            }
+        }
+    }
+    for (int64_t s = 0; s < n_steps; ++s) {
+        if (s > 0) MMF_CUDA(c->stage(STAGE_1, c->U, c->R));
+        MMF_CUDA(c->stage(STAGE_2, c->U, c->W));
+        if (s + 1 < n_steps) {
+            MMF_CUDA(c->stage(STAGE_3, c->U, c->U));
+            continue;
+        }
+        // last step: stage 3, transposition and download, band by band
+        for (int b = 0; b < p.K; ++b) {
+            long long base, count;
+            band_cells(b, base, count);
+            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U));
+            const unsigned blocks = (unsigned)std::min<long long>((count + 255) / 256, 4L * 152);
+            soa_to_aos_band_kernel<<<blocks, 256, 0, c->stream>>>(c->U, c->aos, base, count, plane);
+            ++c->launches;
+            MMF_CUDA(cudaPeekAtLastError());
+            MMF_CUDA(cudaEventRecord(c->ev_dn[b], c->stream));
+            MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_dn[b], 0));
+            MMF_CUDA(cudaMemcpyAsync(aos + NF * base, c->aos + NF * base, sizeof(double) * NF * count,
+                                     cudaMemcpyDeviceToHost, c->copy_stream));
+        }
+    }
+    MMF_CUDA(cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->copy_stream));
+    if (t_out) *t_out = c->h_ctrl->t;
+    if (c->h_ctrl->status) return fail(MMF_ERR_STATE, "non-physical state (negative density/pressure or NaN)");
+    return MMF_OK;
+}
+
+// Chooses the decomposition (2D: rows per marching chunk and warps per block;
+// 3D: planes per chunk) by timing a few steps of each candidate from the
+// current state; the state and the time control are restored afterwards.
+// Every decomposition gives the same bits (each cell's arithmetic is fixed
+// and maxEig is a max), so only the speed changes.
+int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    if (trial_steps < 1) trial_steps = 4;
+    const size_t bytes = sizeof(double) * NF * (size_t)c->gp.plane;
+    Ctrl saved;
+    MMF_CUDA(cudaMemcpyAsync(c->aos, c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    MMF_CUDA(cudaMemcpyAsync(&saved, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    Ctrl trial = saved;
+    trial.t_end = HUGE_VAL;
+    trial.max_steps = LLONG_MAX;
+    std::vector<std::pair<int, int>> cand;
+    if (c->gp.dim == 2) {
+        for (int ch : {8, 12, 16, 20, 24, 28, 30, 32, 40, 48, 64})
+            for (int w : {1, 2, 4}) cand.emplace_back(ch, w);
+    } else {
+        for (int ch : {4, 8, 16, 32, 64}) cand.emplace_back(ch, 0);
+    }
+    const int by = c->grid.order == 2 ? BY3D_O2 : BY3D;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    MMF_CUDA(cudaEventCreate(&e0));
+    MMF_CUDA(cudaEventCreate(&e1));
+    std::pair<int, int> best(c->gp.chunk, c->gp.wpb);
+    float best_ms = 1e30f;
+    cudaError_t e = cudaSuccess;
+    for (const auto &cd : cand) {
+        plan_cartesian(c->gp, cd.first, by, cd.second);
+        e = cudaMemcpyAsync(c->U, c->aos, bytes, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->ctrl, &trial, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = c->rk_step();
+        if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+        for (int s = 0; s < trial_steps && e == cudaSuccess; ++s) e = c->rk_step();
+        if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) break;
+        if (ms < best_ms) { best_ms = ms; best = cd; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    plan_cartesian(c->gp, best.first, by, best.second);
+    if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+    if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
+    MMF_CUDA(e);
+    MMF_CUDA(cudaMemcpyAsync(c->U, c->aos, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    MMF_CUDA(cudaMemcpyAsync(c->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    if (chunk_out) *chunk_out = c->gp.chunk;
+    if (warps_out) *warps_out = c->gp.dim == 2 ? c->gp.wpb : 0;
+    return MMF_OK;
+}
+
 int mmf_advance_host(mmf_ctx *c, double *aos, int64_t n_raw, int64_t n_steps, double *t_out)
 {
-    int rc = mmf_upload_state(c, aos, n_raw);
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
+    if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
+    if (n_steps < 0) return fail(MMF_ERR_ARG, "n_steps < 0");
+    if (pipeline_applies(c, aos, n_steps)) return advance_host_pipelined(c, aos, n_steps, t_out);
+    rc = mmf_upload_state(c, aos, n_raw);
     if (rc) return rc;
     int64_t done = 0;
     rc = mmf_advance(c, n_steps, t_out, &done);

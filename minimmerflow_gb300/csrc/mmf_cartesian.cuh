@@ -52,7 +52,10 @@ struct GridParams {
     int chunk;      // rows (2D) / planes (3D) per marching chunk
     int nseg;       // x segments of 30 cells
     int nrowblk;    // 3D: row blocks in y
-    int nchunk;
+    int nchunk;     // chunks covered by one launch
+    int chunk0;     // first chunk of the launch (a launch may cover a band of the grid)
+    int bookkeep;   // this launch updates the control block (exactly one launch per stage)
+    int wpb;        // 2D: warps per block
     long long plane;  // cells per field plane
 };
 
@@ -350,11 +353,11 @@ __global__ void __launch_bounds__(128) stage2d_kernel(GridParams gp, StageArgs s
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (warp >= gp.nseg * gp.nchunk) return;
     const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (gp.bookkeep && blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
     if (!sc.active) return;
     double lmax = 0.0;
     unsigned status = 0;
-    march2d<A, STAGE>(gp, sa, sc, warp % gp.nseg, warp / gp.nseg, lmax, status);
+    march2d<A, STAGE>(gp, sa, sc, warp % gp.nseg, gp.chunk0 + warp / gp.nseg, lmax, status);
     publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }
 
@@ -380,14 +383,14 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (gp.bookkeep && blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
     if (!sc.active) return;
 
     const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
     int b = blockIdx.x;
     const int seg = b % gp.nseg; b /= gp.nseg;
     const int rb = b % gp.nrowblk; b /= gp.nrowblk;
-    const int chunk = b;
+    const int chunk = gp.chunk0 + b;
     const int x = seg * SEG - 1 + lane;
     const int y = rb * (BY - 2) - 1 + w;
     const int z0 = chunk * gp.chunk;

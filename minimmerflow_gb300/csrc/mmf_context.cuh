@@ -38,8 +38,17 @@ struct mmf_ctx {
     int limit_mode = LIMIT_ALL;
     mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
     float ind_threshold = 0.5f;
+    // pipelined host round trip (mmf_advance_host): a copy stream, one event
+    // per band and direction, pinned host words for the flag and the control block
+    static constexpr int MAX_BANDS = 8;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_up[MAX_BANDS] = {}, ev_dn[MAX_BANDS] = {}, ev_tr = nullptr, ev_flag = nullptr;
+    int *h_flag = nullptr;
+    Ctrl *h_ctrl = nullptr;
 
-    cudaError_t stage(int st, const double *U_in, double *out)
+    cudaError_t stage(int st, const double *U_in, double *out) { return stage_gp(st, gp, U_in, out); }
+    // a stage over the rows (2D) / planes (3D) that 'g' covers
+    cudaError_t stage_gp(int st, const GridParams &g, const double *U_in, double *out)
     {
         StageArgs sa;
         sa.U = U_in;
@@ -49,8 +58,8 @@ struct mmf_ctx {
         sa.ctrl = ctrl;
         sa.rhs_maxeig = rhs_maxeig;
         ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_stage_fast(st, gp, sa, stream, w_zero)
-                                                                : mmf::launch_stage_exact(st, gp, sa, stream);
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_stage_fast(st, g, sa, stream, w_zero)
+                                                                : mmf::launch_stage_exact(st, g, sa, stream);
     }
     cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
     {

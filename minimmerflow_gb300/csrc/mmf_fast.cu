@@ -1,5 +1,8 @@
-// mmf_fast.cu -- fast-arithmetic instantiation of the stage kernels (FMA
-// contraction on; one division and one square root per cell).
+// mmf_fast.cu -- fast-arithmetic instantiation of the stage kernels (one
+// reciprocal and one square root per cell).  Built without implicit FMA
+// contraction: every fused multiply-add is written out, so a cell's bits do
+// not depend on how the compiler unrolled the marching loop, and therefore
+// not on the work decomposition either.
 #include "mmf_batch.cuh"
 #include "mmf_exact_occupancy.h"
 #include "mmf_launch.cuh"

@@ -16,9 +16,12 @@ constexpr int BY3D_O2 = 8;      // warps per 3D order-2 block (face-side records
 
 // Fills the decomposition fields of gp for the given marching chunk; 'by' is
 // the number of warps a 3D block stacks in y (two of them halo rows).
-inline void plan_cartesian(GridParams &gp, int chunk, int by = 16)
+inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0)
 {
     gp.nseg = (gp.n[0] + SEG - 1) / SEG;
+    gp.wpb = (wpb >= 1 && wpb <= WARPS_2D) ? wpb : WARPS_2D;
+    gp.chunk0 = 0;
+    gp.bookkeep = 1;
     if (gp.dim == 2) {
         gp.chunk = chunk > 0 ? chunk : 32;
         gp.nchunk = (gp.n[1] + gp.chunk - 1) / gp.chunk;
@@ -36,7 +39,7 @@ inline long long cartesian_blocks(const GridParams &gp)
 {
     if (gp.dim == 2) {
         long long warps = (long long)gp.nseg * gp.nchunk;
-        return (warps + WARPS_2D - 1) / WARPS_2D;
+        return (warps + gp.wpb - 1) / gp.wpb;
     }
     return (long long)gp.nseg * gp.nrowblk * gp.nchunk;
 }
@@ -46,7 +49,7 @@ inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cud
 {
     const unsigned blocks = (unsigned)cartesian_blocks(gp);
     if (gp.dim == 2) {
-        stage2d_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa);
+        stage2d_kernel<A, STAGE><<<blocks, gp.wpb * 32, 0, s>>>(gp, sa);
     } else {
         if constexpr (HAS3D) stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
         else return cudaErrorInvalidValue;
@@ -80,7 +83,7 @@ inline cudaError_t launch_o2_stage_t(const GridParams &gp, const StageArgs &sa, 
 {
     const unsigned blocks = (unsigned)cartesian_blocks(gp);
     if (gp.dim == 2) {
-        stage2d_o2_kernel<A, STAGE><<<blocks, WARPS_2D * 32, 0, s>>>(gp, sa, oa.state, oa.S);
+        stage2d_o2_kernel<A, STAGE><<<blocks, gp.wpb * 32, 0, s>>>(gp, sa, oa.state, oa.S);
     } else {
         if constexpr (HAS3D) stage3d_o2_kernel<A, STAGE, BY3D_O2><<<blocks, BY3D_O2 * 32, 0, s>>>(gp, sa, oa.state, oa.S);
         else return cudaErrorInvalidValue;

@@ -194,6 +194,13 @@ class CartesianEuler:
     def launch_count(self):
         return self._lib.mmf_launch_count(self._ctx)
 
+    def autotune(self, trial_steps=4):
+        """Pick the stage kernels' decomposition by timing (state restored);
+        returns (chunk, warps_per_block)."""
+        ch, w = C.c_int(), C.c_int()
+        capi.check(self._lib.mmf_autotune(self._ctx, trial_steps, C.byref(ch), C.byref(w)))
+        return ch.value, w.value
+
     def init_state(self, case):
         """Initial state of a problem case computed on the device (problem.cpp:247-392)."""
         capi.check(self._lib.mmf_init_state(self._ctx, C.byref(problem_struct(case))))

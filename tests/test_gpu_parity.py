@@ -277,3 +277,29 @@ def test_status_reports_negative_pressure(mmf):
             s.advance(1)
         assert ei.value.code == mmf.capi.MMF_ERR_STATE
         assert s.status() & 2
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (3, 1), (2, 2)])
+def test_autotune_keeps_state_and_bits(mmf, dim, order):
+    """mmf_autotune restores the state and the time control, and the chosen
+    decomposition gives the same bits as the default one."""
+    P = mmf.problem
+    case = P.radial_sod_2d(96, t_end=0.05) if dim == 2 else P.radial_sod_ratios(24, 10.0, 4.0, dim=3)
+    U0 = case.initial_state()
+    outs = []
+    for tune in (False, True):
+        with case.solver(order=order) as s:
+            s.upload(U0)
+            s.time_setup(0.4, 0.0, math.inf, 12)
+            s.advance(3)
+            if tune:
+                before = s.download()
+                t_before = s.time_info()
+                chunk, wpb = s.autotune(trial_steps=2)
+                assert chunk > 0 and (wpb > 0) == (dim == 2)
+                assert s.time_info() == t_before
+                np.testing.assert_array_equal(s.download(), before)
+            t, steps = s.advance(100)
+            outs.append((s.download(), t, steps))
+    assert outs[0][1:] == outs[1][1:] and outs[0][2] == 9
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
