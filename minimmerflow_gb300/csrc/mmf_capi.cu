@@ -207,14 +207,16 @@ int mmf_destroy(mmf_ctx *c)
     cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
-        for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
-            if (c->ev_up[b]) cudaEventDestroy(c->ev_up[b]);
-            if (c->ev_dn[b]) cudaEventDestroy(c->ev_dn[b]);
-        }
-        if (c->ev_tr) cudaEventDestroy(c->ev_tr);
-        if (c->ev_flag) cudaEventDestroy(c->ev_flag);
         cudaStreamDestroy(c->copy_stream);
     }
+    for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
+        if (c->band_stream[b]) { cudaStreamSynchronize(c->band_stream[b]); cudaStreamDestroy(c->band_stream[b]); }
+        cudaEvent_t evs[4] = {c->ev_up[b], c->ev_tr[b], c->ev_s1[b], c->ev_dn[b]};
+        for (cudaEvent_t e : evs) if (e) cudaEventDestroy(e);
+    }
+    if (c->ev_start) cudaEventDestroy(c->ev_start);
+    if (c->ev_s2) cudaEventDestroy(c->ev_s2);
+    if (c->ev_flag) cudaEventDestroy(c->ev_flag);
     cudaFreeHost(c->h_flag);
     cudaFreeHost(c->h_ctrl);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -657,7 +659,11 @@ void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
 // band's stage 3 is followed by its transposition and its download (copy
 // stream), which overlaps the stage 3 of the next band.  Stage 2 needs the
 // step's dt, a max over every cell of stage 1, so it runs on the whole grid.
-// Band launches use shorter marching chunks so that each one fills the GPU.
+// The stage-1 band kernels run on one stream per band (band 0 at the highest
+// priority) so that they overlap one another and the transpositions; the
+// stage-3 bands run in order on one stream so that the first downloads start
+// early.  Band launches use shorter marching chunks so that each has work for
+// every SM.
 struct BandPlan {
     int K = 0;
     int rows = 0;          // rows (planes) per band, a multiple of chunk
@@ -673,10 +679,10 @@ static BandPlan band_plan(const mmf_ctx *c)
     p.n_slow = gp.dim == 2 ? gp.n[1] : gp.n[2];
     p.slab = gp.dim == 2 ? (long long)gp.n[0] : (long long)gp.n[0] * gp.n[1];
     if (p.n_slow < 64 || p.slab * p.n_slow < (1 << 18)) return p;   // too small to pay
-    int K = 4;
+    int K = 8;
     int rows = (p.n_slow + K - 1) / K;
     int ch;
-    if (gp.dim == 2) ch = (int)std::min<long long>(32, std::max<long long>(4, (long long)gp.nseg * rows / 1216));
+    if (gp.dim == 2) ch = (int)std::min<long long>(32, std::max<long long>(4, (long long)gp.nseg * rows / 2432));
     else ch = (int)std::min<long long>(32, std::max<long long>(2, (long long)gp.nseg * gp.nrowblk * rows / 304));
     rows = (rows + ch - 1) / ch * ch;
     p.K = (p.n_slow + rows - 1) / rows;
@@ -699,12 +705,19 @@ static GridParams band_params(const mmf_ctx *c, const BandPlan &p, int b, int bo
 static int pipeline_resources(mmf_ctx *c)
 {
     if (c->copy_stream) return MMF_OK;
+    int least = 0, greatest = 0;
+    MMF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     MMF_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
+        const int prio = std::min(least, greatest + b);   // greatest is the numerically lowest
+        MMF_CUDA(cudaStreamCreateWithPriority(&c->band_stream[b], cudaStreamNonBlocking, prio));
         MMF_CUDA(cudaEventCreateWithFlags(&c->ev_up[b], cudaEventDisableTiming));
+        MMF_CUDA(cudaEventCreateWithFlags(&c->ev_tr[b], cudaEventDisableTiming));
+        MMF_CUDA(cudaEventCreateWithFlags(&c->ev_s1[b], cudaEventDisableTiming));
         MMF_CUDA(cudaEventCreateWithFlags(&c->ev_dn[b], cudaEventDisableTiming));
     }
-    MMF_CUDA(cudaEventCreateWithFlags(&c->ev_tr, cudaEventDisableTiming));
+    MMF_CUDA(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
+    MMF_CUDA(cudaEventCreateWithFlags(&c->ev_s2, cudaEventDisableTiming));
     MMF_CUDA(cudaEventCreateWithFlags(&c->ev_flag, cudaEventDisableTiming));
     MMF_CUDA(cudaHostAlloc(&c->h_flag, sizeof(int), cudaHostAllocDefault));
     MMF_CUDA(cudaHostAlloc(&c->h_ctrl, sizeof(Ctrl), cudaHostAllocDefault));
@@ -714,7 +727,8 @@ static int pipeline_resources(mmf_ctx *c)
 static bool pipeline_applies(const mmf_ctx *c, const double *aos, int64_t n_steps)
 {
     if (c->grid.order != 1 || c->raw_to_cell || n_steps < 1) return false;
-    if (band_plan(c).K < 2 || band_plan(c).K > mmf_ctx::MAX_BANDS) return false;
+    const BandPlan p = band_plan(c);
+    if (p.K < 2 || p.K > mmf_ctx::MAX_BANDS) return false;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, aos) != cudaSuccess) { cudaGetLastError(); return false; }
     return a.type == cudaMemoryTypeHost;   // page-locked: the copies run asynchronously
@@ -734,13 +748,13 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
         base = (long long)r0 * p.slab;
         count = (long long)(r1 - r0) * p.slab;
     };
-    // band b's stage 1 needs the bands on both sides of it on the device
-    auto need = [&](int b) { return (b == 0 && periodic_slow) ? p.K - 1 : std::min(b + 1, p.K - 1); };
+    auto tr_blocks = [](long long count) { return (unsigned)std::min<long long>((count + 255) / 256, 4L * 152); };
 
-    // upload, transposition and stage 1, band by band
+    // upload and transposition, band by band; the device buffers are free once
+    // the work enqueued before this call has run
     MMF_CUDA(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
-    MMF_CUDA(cudaEventRecord(c->ev_tr, c->stream));
-    MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr, 0));   // the device buffers are free
+    MMF_CUDA(cudaEventRecord(c->ev_start, c->stream));
+    MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_start, 0));
     for (int b = 0; b < p.K; ++b) {
         long long base, count;
         band_cells(b, base, count);
@@ -748,33 +762,33 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
                                  cudaMemcpyHostToDevice, c->copy_stream));
         MMF_CUDA(cudaEventRecord(c->ev_up[b], c->copy_stream));
     }
-    int launched = 0;   // bands whose stage 1 is enqueued (in order, except band 0 when periodic)
-    std::vector<char> s1((size_t)p.K, 0);
     for (int b = 0; b < p.K; ++b) {
         long long base, count;
         band_cells(b, base, count);
         MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_up[b], 0));
-        const unsigned blocks = (unsigned)std::min<long long>((count + 255) / 256, 4L * 152);
-        aos_to_soa_band_kernel<<<blocks, 256, 0, c->stream>>>(c->aos, c->U, base, count, plane,
-                                                              check_w ? c->flag : nullptr);
+        aos_to_soa_band_kernel<<<tr_blocks(count), 256, 0, c->stream>>>(c->aos, c->U, base, count, plane,
+                                                                         check_w ? c->flag : nullptr);
         ++c->launches;
         MMF_CUDA(cudaPeekAtLastError());
-        if (b == p.K - 1 && check_w) {
-            MMF_CUDA(cudaEventRecord(c->ev_tr, c->stream));
-            MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr, 0));
-            MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
-            MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
-        }
-        for (int q = 0; q < p.K; ++q)
-            if (!s1[(size_t)q] && need(q) <= b) {
-                MMF_CUDA(c->stage_gp(STAGE_1, band_params(c, p, q, 1), c->U, c->R));
-                s1[(size_t)q] = 1;
-                ++launched;
-            }
+        MMF_CUDA(cudaEventRecord(c->ev_tr[b], c->stream));
     }
     if (check_w) {
-        // the stage-1 kernels assumed the previous z-momentum decision; redo
-        // stage 1 on the whole grid if this state does not fit it
+        MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr[p.K - 1], 0));
+        MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
+        MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
+    }
+    // stage 1 of band q once the bands on both sides of it are on the device
+    // (the transpositions run in band order, so the last one it needs suffices)
+    for (int q = 0; q < p.K; ++q) {
+        const int need = (q == 0 && periodic_slow) ? p.K - 1 : std::min(q + 1, p.K - 1);
+        MMF_CUDA(cudaStreamWaitEvent(c->band_stream[q], c->ev_tr[need], 0));
+        MMF_CUDA(c->stage_gp(STAGE_1, band_params(c, p, q, q == 0), c->U, c->R, c->band_stream[q]));
+        MMF_CUDA(cudaEventRecord(c->ev_s1[q], c->band_stream[q]));
+    }
+    for (int q = 0; q < p.K; ++q) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_s1[q], 0));
+    if (check_w) {
+        // the stage-1 kernels used the previous z-momentum choice; redo stage 1
+        // on the whole grid if this state does not fit it
         MMF_CUDA(cudaEventSynchronize(c->ev_flag));
         const bool wz = (*c->h_flag == 0);
         if (wz != c->w_zero) {
@@ -796,13 +810,13 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             MMF_CUDA(c->stage(STAGE_3, c->U, c->U));
             continue;
         }
-        // last step: stage 3, transposition and download, band by band
+        // last step: stage 3, transposition and download, band by band, in
+        // band order on the compute stream so that the downloads start early
         for (int b = 0; b < p.K; ++b) {
             long long base, count;
             band_cells(b, base, count);
-            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U));
-            const unsigned blocks = (unsigned)std::min<long long>((count + 255) / 256, 4L * 152);
-            soa_to_aos_band_kernel<<<blocks, 256, 0, c->stream>>>(c->U, c->aos, base, count, plane);
+            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U, c->stream));
+            soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, c->stream>>>(c->U, c->aos, base, count, plane);
             ++c->launches;
             MMF_CUDA(cudaPeekAtLastError());
             MMF_CUDA(cudaEventRecord(c->ev_dn[b], c->stream));

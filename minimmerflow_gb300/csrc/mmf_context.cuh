@@ -42,13 +42,15 @@ struct mmf_ctx {
     // per band and direction, pinned host words for the flag and the control block
     static constexpr int MAX_BANDS = 8;
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_up[MAX_BANDS] = {}, ev_dn[MAX_BANDS] = {}, ev_tr = nullptr, ev_flag = nullptr;
+    cudaStream_t band_stream[MAX_BANDS] = {};   // band b at priority b (band 0 first)
+    cudaEvent_t ev_up[MAX_BANDS] = {}, ev_tr[MAX_BANDS] = {}, ev_s1[MAX_BANDS] = {}, ev_dn[MAX_BANDS] = {};
+    cudaEvent_t ev_start = nullptr, ev_s2 = nullptr, ev_flag = nullptr;
     int *h_flag = nullptr;
     Ctrl *h_ctrl = nullptr;
 
-    cudaError_t stage(int st, const double *U_in, double *out) { return stage_gp(st, gp, U_in, out); }
-    // a stage over the rows (2D) / planes (3D) that 'g' covers
-    cudaError_t stage_gp(int st, const GridParams &g, const double *U_in, double *out)
+    cudaError_t stage(int st, const double *U_in, double *out) { return stage_gp(st, gp, U_in, out, stream); }
+    // a stage over the rows (2D) / planes (3D) that 'g' covers, on stream 'on'
+    cudaError_t stage_gp(int st, const GridParams &g, const double *U_in, double *out, cudaStream_t on)
     {
         StageArgs sa;
         sa.U = U_in;
@@ -58,8 +60,8 @@ struct mmf_ctx {
         sa.ctrl = ctrl;
         sa.rhs_maxeig = rhs_maxeig;
         ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_stage_fast(st, g, sa, stream, w_zero)
-                                                                : mmf::launch_stage_exact(st, g, sa, stream);
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_stage_fast(st, g, sa, on, w_zero)
+                                                                : mmf::launch_stage_exact(st, g, sa, on);
     }
     cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
     {

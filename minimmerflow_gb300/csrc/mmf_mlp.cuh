@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();
     const uint32_t tmem = tmem_base;
-    const int warp = tid >> 5, lane = tid & 31;
+    const int warp = tid >> 5;
     const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
     const uint32_t idesc = umma_idesc(MLP_TILE, MLP_H);
     const long long ntiles = (gp.plane + MLP_TILE - 1) / MLP_TILE;
