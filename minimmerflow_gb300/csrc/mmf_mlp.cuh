@@ -64,27 +64,6 @@ __device__ __forceinline__ float gelu_grad(float x)
 }
 __device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
-// FP64 -> FP32 by truncating the mantissa, on the integer pipe: a stencil of
-// 27 cells needs 135 conversions per cell, and the FP64 unit that converts
-// is the feature gather's bottleneck.  Below the FP32 range the result is a
-// signed zero, above it a signed infinity; NaN stays NaN.  The features are
-// rounded to BF16 afterwards, so truncation instead of rounding is invisible.
-__device__ __forceinline__ float f64_to_f32_trunc(double d)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned sign = hi & 0x80000000u;
-    const int ef = (int)((hi >> 20) & 0x7ffu);
-    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const int e = ef - 1023 + 127;
-    unsigned r;
-    if (ef == 0x7ff) r = sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u);
-    else if (e <= 0) r = sign;
-    else if (e >= 255) r = sign | 0x7f800000u;
-    else r = sign | ((unsigned)e << 23) | mant;
-    return __uint_as_float(r);
-}
-
 // Primitive variables (rho, u, v, w, p) of the cell at (x, y, z), border wrap or clamp.
 __device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, int x, int y, int z, float *q)
 {
@@ -95,11 +74,11 @@ __device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, i
     z = z < 0 ? (pz ? nz - 1 : 0) : (z >= nz ? (pz ? 0 : nz - 1) : z);
     const long long g = (long long)x + (long long)nx * ((long long)y + (long long)ny * z);
     const long long n = gp.plane;
-    const float rho = f64_to_f32_trunc(__ldg(U + g));
+    const float rho = (float)__ldg(U + g);
     const float ri = 1.0f / rho;
-    const float u = f64_to_f32_trunc(__ldg(U + n + g)) * ri, v = f64_to_f32_trunc(__ldg(U + 2 * n + g)) * ri,
-                w = f64_to_f32_trunc(__ldg(U + 3 * n + g)) * ri;
-    const float E = f64_to_f32_trunc(__ldg(U + 4 * n + g));
+    const float u = (float)__ldg(U + n + g) * ri, v = (float)__ldg(U + 2 * n + g) * ri,
+                w = (float)__ldg(U + 3 * n + g) * ri;
+    const float E = (float)__ldg(U + 4 * n + g);
     q[0] = rho;
     q[1] = u;
     q[2] = v;

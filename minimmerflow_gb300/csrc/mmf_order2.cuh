@@ -66,9 +66,21 @@ __device__ __forceinline__ bool admissible(const double *c)
 {
     constexpr int NV = A::NVAR;
     if (!(c[0] > 0.0)) return false;
-    double m2 = c[1] * c[1] + c[2] * c[2];
-    if (NV == 5) m2 = m2 + c[3] * c[3];
-    return (2.0 * c[0] * c[NV - 1] - m2) > 0.0;
+    if (IsExact<A>::value) {
+        double m2 = c[1] * c[1] + c[2] * c[2];
+        if (NV == 5) m2 = m2 + c[3] * c[3];
+        return (2.0 * c[0] * c[NV - 1] - m2) > 0.0;
+    }
+    double m2 = fma(c[2], c[2], c[1] * c[1]);
+    if (NV == 5) m2 = fma(c[3], c[3], m2);
+    return fma(2.0 * c[0], c[NV - 1], -m2) > 0.0;
+}
+
+// reconstructed face state U + off sigma (off = +-1/2)
+template <class A>
+__device__ __forceinline__ double face_value(double u, double off, double sigma)
+{
+    return IsExact<A>::value ? u + off * sigma : fma(off, sigma, u);
 }
 
 template <class A>
@@ -134,7 +146,10 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
         for (int d = 0; d < DIM; ++d) {
             double fm[NV], fp[NV];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) { fm[k] = uc[k] - 0.5 * sig[d][k]; fp[k] = uc[k] + 0.5 * sig[d][k]; }
+            for (int k = 0; k < NV; ++k) {
+                fm[k] = IsExact<A>::value ? uc[k] - 0.5 * sig[d][k] : fma(-0.5, sig[d][k], uc[k]);
+                fp[k] = face_value<A>(uc[k], 0.5, sig[d][k]);
+            }
             ok = ok && admissible<A>(fm) && admissible<A>(fp);
         }
         if (!ok) {
@@ -245,7 +260,7 @@ __device__ __forceinline__ void load_sides(const GridParams &gp, const double *s
                 double fs[NV];
                 const double off = s ? 0.5 : -0.5;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) fs[k] = uc[k] + off * sg[d][k];
+                for (int k = 0; k < NV; ++k) fs[k] = face_value<A>(uc[k], off, sg[d][k]);
                 side_record<A, DIM>(fs, d, sr.r[d][s], s == 1 ? status : nullptr);
             }
         return;
@@ -256,7 +271,7 @@ __device__ __forceinline__ void load_sides(const GridParams &gp, const double *s
     double fs[NV], gs[NV];
     const double off = gh[gdir] > 0 ? 0.5 : -0.5;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) fs[k] = uc[k] + off * sg[gdir][k];
+    for (int k = 0; k < NV; ++k) fs[k] = face_value<A>(uc[k], off, sg[gdir][k]);
     double nrm[3] = {0.0, 0.0, 0.0};
     nrm[gdir] = (double)gh[gdir];
     ghost_state<A>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], nrm, fs, gp.dir_prim, gs);
