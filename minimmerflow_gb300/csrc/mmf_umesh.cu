@@ -64,6 +64,7 @@ struct mmf_umesh {
     long long *owner = nullptr, *neigh = nullptr, *csr_off = nullptr, *csr_face = nullptr;
     int *bc = nullptr;
     double *U = nullptr, *R = nullptr, *W = nullptr, *P = nullptr, *S = nullptr, *aos = nullptr;
+    double *rec = nullptr;    // fast arithmetic: 6 record planes
     Ctrl *ctrl = nullptr;
     double *rhs_maxeig = nullptr;
     cudaGraphExec_t g_many = nullptr, g_one = nullptr;
@@ -74,10 +75,13 @@ struct mmf_umesh {
     cudaError_t face(const double *state)
     {
         ++launches;
-        if (arith == MMF_ARITH_FAST && STAGE != STAGE_RHS)
+        if (arith == MMF_ARITH_FAST && STAGE != STAGE_RHS) {
+            urec_kernel<<<grid_for(m.ncells), 256, 0, stream>>>(m, state, ctrl, STAGE);
+            ++launches;
             uface_kernel<FastArith, STAGE><<<grid_for(m.nfaces), 256, 0, stream>>>(m, state, P, ctrl, rhs_maxeig);
-        else
+        } else {
             uface_kernel<ExactArith, STAGE><<<grid_for(m.nfaces), 256, 0, stream>>>(m, state, P, ctrl, rhs_maxeig);
+        }
         return cudaPeekAtLastError();
     }
     template <int STAGE>
@@ -90,6 +94,8 @@ struct mmf_umesh {
             ucell_kernel<ExactArith, STAGE><<<grid_for(m.ncells), 256, 0, stream>>>(m, P, U, state, out, ctrl);
         return cudaPeekAtLastError();
     }
+    // face (+ record) and cell kernels of three stages and the W1 kernel
+    int launches_per_step() const { return arith == MMF_ARITH_FAST ? 10 : 7; }
     cudaError_t rk_step()
     {
         cudaError_t e;
@@ -190,6 +196,7 @@ int mmf_umesh_create(const mmf_umesh_desc *d, int device, mmf_umesh **out)
     A((void **)&u->S, sb);
     A((void **)&u->aos, sb);
     A((void **)&u->P, sizeof(double) * NF * nf);
+    if (d->arith == MMF_ARITH_FAST) A((void **)&u->rec, sizeof(double) * 6 * n);
     A((void **)&u->ctrl, sizeof(Ctrl));
     A((void **)&u->rhs_maxeig, sizeof(double));
     auto H = [&](void *dst, const void *src, size_t b) { if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, u->stream); };
@@ -223,6 +230,7 @@ int mmf_umesh_create(const mmf_umesh_desc *d, int device, mmf_umesh **out)
     m.bc = u->bc;
     m.csr_off = u->csr_off;
     m.csr_face = u->csr_face;
+    m.rec = u->rec;
     for (int k = 0; k < NF; ++k) m.dir_prim[k] = d->dirichlet_prim[k];
     *out = u;
     return MMF_OK;
@@ -238,7 +246,7 @@ int mmf_umesh_destroy(mmf_umesh *u)
     cudaFree(u->vol); cudaFree(u->solved); cudaFree(u->owner); cudaFree(u->neigh); cudaFree(u->area);
     cudaFree(u->normal); cudaFree(u->bc); cudaFree(u->csr_off); cudaFree(u->csr_face);
     cudaFree(u->U); cudaFree(u->R); cudaFree(u->W); cudaFree(u->S); cudaFree(u->aos); cudaFree(u->P);
-    cudaFree(u->ctrl); cudaFree(u->rhs_maxeig);
+    cudaFree(u->ctrl); cudaFree(u->rhs_maxeig); cudaFree(u->rec);
     if (u->stream) cudaStreamDestroy(u->stream);
     delete u;
     return MMF_OK;
@@ -324,12 +332,12 @@ int mmf_umesh_advance(mmf_umesh *u, int64_t n_steps, double *t_out, int64_t *ste
     int64_t left = n_steps;
     while (left >= GRAPH_STEPS) {
         UM_CUDA(cudaGraphLaunch(u->g_many, u->stream));
-        u->launches += 7 * GRAPH_STEPS;
+        u->launches += u->launches_per_step() * GRAPH_STEPS;
         left -= GRAPH_STEPS;
     }
     while (left-- > 0) {
         UM_CUDA(cudaGraphLaunch(u->g_one, u->stream));
-        u->launches += 7;
+        u->launches += u->launches_per_step();
     }
     UM_CUDA(cudaMemcpyAsync(&after, u->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, u->stream));
     UM_CUDA(cudaStreamSynchronize(u->stream));

@@ -5,6 +5,9 @@
 // (BC_WALL faces between fluid and solid cells, main.cpp:251-277), the
 // forward-facing step's Dirichlet / free-flow / reflecting borders.
 //
+//   urec_kernel    fast arithmetic: the per-cell record (u, v, w, p, sound
+//                  speed, rho H) of the stage input, once per cell, so that
+//                  the face kernel converts no interior state.
 //   uface_kernel   one thread per interface: the face states (order 1: the
 //                  cell means; a border or wall face: the ghost of the fluid
 //                  side with the normal flipped when the neighbour is the
@@ -34,6 +37,7 @@ struct UMesh {
     const int *bc;                // per face (BC_NONE interior)
     const long long *csr_off;     // per cell: [off[c], off[c+1]) into csr_face
     const long long *csr_face;    // face index, negated - 1 when the cell is the owner
+    double *rec;                  // fast arithmetic: per-cell record, 6 planes (u, v, w, p, a, rho H)
     double dir_prim[NF];
 };
 
@@ -44,43 +48,73 @@ __device__ __forceinline__ void uload(const double *S, long long n, long long c,
     for (int k = 0; k < NF; ++k) u[k] = __ldg(S + k * n + c);
 }
 
-template <class A>
-__device__ __forceinline__ double usplit(const double *cl, const double *cr, const double *nrm, double *F)
+// Fast arithmetic: the record of a state (one reciprocal and one square root).
+__device__ __forceinline__ void fast_record(const double *c, double *r)
 {
-    if (IsExact<A>::value) {
-        // euler.cpp:42-73
-        double pl[NF], pr[NF], fl[NF], fr[NF];
-        ExactArith::cons2prim(cl, pl);
-        ExactArith::cons2prim(cr, pr);
-        ExactArith::eval_fluxes(cl, pl, nrm, fl);
-        ExactArith::eval_fluxes(cr, pr, nrm, fr);
-        const double lamL = fabs(ExactArith::normal_velocity(pl, nrm)) + sqrt(GAMMA * pl[4]);
-        const double lamR = fabs(ExactArith::normal_velocity(pr, nrm)) + sqrt(GAMMA * pr[4]);
-        return ExactArith::face(cl, fl, lamL, cr, fr, lamR, F);
-    } else {
-        // fast: one reciprocal and one square root per side, flux along n
-        double f[2][NF], lam[2];
-        const double *cs[2] = {cl, cr};
+    const double ri = rcp_newton(c[0]);
+    const double u = c[1] * ri, v = c[2] * ri, w = c[3] * ri;
+    const double p = (GAMMA - 1.0) * fma(-0.5, fma(c[3], w, fma(c[2], v, c[1] * u)), c[4]);
+    r[0] = u;
+    r[1] = v;
+    r[2] = w;
+    r[3] = p;
+    r[4] = sqrt_newton(GAMMA * p * ri);
+    r[5] = c[4] + p;
+}
+
+// Fast arithmetic: the LLF flux (times half the area) of a face from the two
+// sides' states and records; returns the face eigenvalue.
+__device__ __forceinline__ double fast_split(const double *cl, const double *rl, const double *cr, const double *rr,
+                                             const double *nrm, double half_area, double *F)
+{
+    double f[2][NF], lam[2];
+    const double *cs[2] = {cl, cr}, *rs[2] = {rl, rr};
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const double *c = cs[s];
-            const double ri = rcp_newton(c[0]);
-            const double u = c[1] * ri, v = c[2] * ri, w = c[3] * ri;
-            const double p = (GAMMA - 1.0) * fma(-0.5, fma(c[3], w, fma(c[2], v, c[1] * u)), c[4]);
-            const double a = sqrt_newton(GAMMA * p * ri);
-            const double un = fma(w, nrm[2], fma(v, nrm[1], u * nrm[0]));
-            const double mn = c[0] * un;
-            f[s][0] = mn;
-            f[s][1] = fma(mn, u, p * nrm[0]);
-            f[s][2] = fma(mn, v, p * nrm[1]);
-            f[s][3] = fma(mn, w, p * nrm[2]);
-            f[s][4] = un * (c[4] + p);
-            lam[s] = fabs(un) + a;
-        }
-        const double lambda = max_nonneg(lam[0], lam[1]);
+    for (int s = 0; s < 2; ++s) {
+        const double *c = cs[s], *r = rs[s];
+        const double un = fma(r[2], nrm[2], fma(r[1], nrm[1], r[0] * nrm[0]));
+        const double mn = c[0] * un;
+        f[s][0] = mn;
+        f[s][1] = fma(mn, r[0], r[3] * nrm[0]);
+        f[s][2] = fma(mn, r[1], r[3] * nrm[1]);
+        f[s][3] = fma(mn, r[2], r[3] * nrm[2]);
+        f[s][4] = un * r[5];
+        lam[s] = fabs(un) + r[4];
+    }
+    const double lambda = max_nonneg(lam[0], lam[1]);
 #pragma unroll
-        for (int k = 0; k < NF; ++k) F[k] = 0.5 * fma(-lambda, cr[k] - cl[k], f[0][k] + f[1][k]);
-        return lambda;
+    for (int k = 0; k < NF; ++k) F[k] = half_area * fma(-lambda, cr[k] - cl[k], f[0][k] + f[1][k]);
+    return lambda;
+}
+
+// Reference arithmetic: euler.cpp:42-73 on the two side states.
+__device__ __forceinline__ double exact_split(const double *cl, const double *cr, const double *nrm, double *F)
+{
+    double pl[NF], pr[NF], fl[NF], fr[NF];
+    ExactArith::cons2prim(cl, pl);
+    ExactArith::cons2prim(cr, pr);
+    ExactArith::eval_fluxes(cl, pl, nrm, fl);
+    ExactArith::eval_fluxes(cr, pr, nrm, fr);
+    const double lamL = fabs(ExactArith::normal_velocity(pl, nrm)) + sqrt(GAMMA * pl[4]);
+    const double lamR = fabs(ExactArith::normal_velocity(pr, nrm)) + sqrt(GAMMA * pr[4]);
+    return ExactArith::face(cl, fl, lamL, cr, fr, lamR, F);
+}
+
+// Fast arithmetic: the record planes of every cell of the stage input.
+__global__ void __launch_bounds__(256) urec_kernel(UMesh m, const double *state, const Ctrl *ctrl, int stage)
+{
+    if (stage >= STAGE_1) {
+        const bool active = (stage == STAGE_1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps)
+                                               : ctrl->active != 0;
+        if (!active) return;
+    }
+    const long long n = m.ncells;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        double u[NF], r[6];
+        uload(state, n, c, u);
+        fast_record(u, r);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) m.rec[k * n + c] = r[k];
     }
 }
 
@@ -102,23 +136,39 @@ __global__ void __launch_bounds__(256) uface_kernel(UMesh m, const double *state
         double F[NF] = {0.0, 0.0, 0.0, 0.0, 0.0};
         if (os || ns) {
             const double nrm[3] = {__ldg(m.normal + f), __ldg(m.normal + nf + f), __ldg(m.normal + 2 * nf + f)};
-            double co[NF], cn[NF];
+            double co[NF], cn[NF], ro[6], rn[6];
             const int bc = m.bc[f];
             if (bc == BC_NONE) {
                 uload(state, n, o, co);
                 uload(state, n, nb, cn);
+                if (!IsExact<A>::value) {
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) { ro[k] = __ldg(m.rec + k * n + o); rn[k] = __ldg(m.rec + k * n + nb); }
+                }
             } else {
                 double n2[3] = {nrm[0], nrm[1], nrm[2]};
                 double *fluid = os ? co : cn, *virt = os ? cn : co;
                 if (!os) { n2[0] = -1. * n2[0]; n2[1] = -1. * n2[1]; n2[2] = -1. * n2[2]; }
-                uload(state, n, os ? o : nb, fluid);
+                const long long fc = os ? o : nb;
+                uload(state, n, fc, fluid);
                 ghost_state<ExactArith>(bc, n2, fluid, m.dir_prim, virt);
-            }
-            const double lam = usplit<A>(co, cn, nrm, F);
-            lmax = max_nonneg(lmax, lam);
-            const double ar = __ldg(m.area + f);
+                if (!IsExact<A>::value) {
+                    double *rf = os ? ro : rn, *rv = os ? rn : ro;
 #pragma unroll
-            for (int k = 0; k < NF; ++k) F[k] = ar * F[k];
+                    for (int k = 0; k < 6; ++k) rf[k] = __ldg(m.rec + k * n + fc);
+                    fast_record(virt, rv);
+                }
+            }
+            const double ar = __ldg(m.area + f);
+            double lam;
+            if (IsExact<A>::value) {
+                lam = exact_split(co, cn, nrm, F);
+#pragma unroll
+                for (int k = 0; k < NF; ++k) F[k] = ar * F[k];
+            } else {
+                lam = fast_split(co, ro, cn, rn, nrm, 0.5 * ar, F);
+            }
+            lmax = max_nonneg(lmax, lam);
         }
 #pragma unroll
         for (int k = 0; k < NF; ++k) P[k * nf + f] = F[k];
