@@ -86,7 +86,11 @@ __device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, i
     q[4] = (float)(GAMMA - 1.0) * (E - 0.5f * rho * (u * u + v * v + w * w));
 }
 
+template <int DIM, class Put>
+__device__ __forceinline__ void stencil_features(float (*q)[5], Put put);
+
 // The KPAD features of grid cell g (FP32), written through 'put(k, value)'.
+// Stencil cell s is at (dx, dy, dz) = (s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1).
 template <int DIM, class Put>
 __device__ __forceinline__ void cell_features(const double *U, const GridParams &gp, long long g, Put put)
 {
@@ -99,6 +103,44 @@ __device__ __forceinline__ void cell_features(const double *U, const GridParams 
         const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
         prim_at(U, gp, x + dx, y + dy, z + dz, q[s]);
     }
+    stencil_features<DIM>(q, put);
+}
+
+// Primitive strip of a tile of MLP_TILE cells that lie in one grid row
+// (x0 .. x0 + MLP_TILE - 1 at row y, plane z): for each of the 3^(DIM-1)
+// (dy, dz) rows of the stencil, the MLP_TILE + 2 cells x0 - 1 .. x0 + MLP_TILE,
+// each converted once (instead of once per stencil that contains it).
+// sQ[(r * (MLP_TILE + 2) + j) * 5 + v], r = (dy + 1) + 3 (dz + 1).
+template <int DIM>
+__device__ __forceinline__ void tile_strip(const double *U, const GridParams &gp, int x0, int y, int z, int tid, float *sQ)
+{
+    constexpr int NR = DIM == 3 ? 9 : 3;
+#pragma unroll 1
+    for (int r = 0; r < NR; ++r) {
+        const int dy = r % 3 - 1, dz = DIM == 3 ? r / 3 - 1 : 0;
+        prim_at(U, gp, x0 - 1 + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + tid) * 5);
+        if (tid < 2) prim_at(U, gp, x0 - 1 + MLP_TILE + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + MLP_TILE + tid) * 5);
+    }
+}
+
+// The features of the tile's cell 'tid' from the strip.
+template <int DIM, class Put>
+__device__ __forceinline__ void strip_features(const float *sQ, int tid, Put put)
+{
+    constexpr int NS = DIM == 3 ? 27 : 9;
+    float q[NS][5];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) q[s][v] = sQ[((s / 3) * (MLP_TILE + 2) + tid + s % 3) * 5 + v];
+    stencil_features<DIM>(q, put);
+}
+
+// Normalised stencil differences of the primitives q[s][v] (FP32).
+template <int DIM, class Put>
+__device__ __forceinline__ void stencil_features(float (*q)[5], Put put)
+{
+    constexpr int NS = DIM == 3 ? 27 : 9;
     constexpr int C = DIM == 3 ? 13 : 4;   // centre of the stencil
     const float a_c = sqrtf(fmaxf((float)GAMMA * q[C][4] / q[C][0], 0.0f));
 #pragma unroll
@@ -199,6 +241,13 @@ struct MlpDev {
     const float *params;        // FP32 parameters (biases, w3, b3 are read from here)
 };
 
+// The tile's MLP_TILE cells lie in one grid row (the strip path applies).
+__device__ __forceinline__ bool tile_in_row(const GridParams &gp, long long tile)
+{
+    const long long g0 = tile * MLP_TILE;
+    return g0 % gp.n[0] + MLP_TILE <= gp.n[0] && g0 + MLP_TILE <= gp.plane;
+}
+
 // Fused features + MLP over the cells of a grid (persistent, one 128-cell tile
 // per iteration).  prob (nullable) receives y, flags (nullable) y > threshold.
 // Returns through *err a non-zero code if an MMA completion wait gave up.
@@ -213,6 +262,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     __nv_bfloat16 *sW1 = sX + MLP_TILE * KP;                             // 64 x KP
     __nv_bfloat16 *sH = sW1 + MLP_H * KP;                                // 128 x 64
     __nv_bfloat16 *sW2 = sH + MLP_TILE * MLP_H;                          // 64 x 64
+    float *sQ = reinterpret_cast<float *>(sW2 + MLP_H * MLP_H);          // primitive strip of a tile
     __shared__ __align__(8) uint64_t mbar_mma;
     __shared__ __align__(8) uint64_t mbar_load;
     __shared__ uint32_t tmem_base;
@@ -270,6 +320,13 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
             const long long off = bg.offsets[c];
             cell_features<DIM>(U + off, bg.cases[c].gp, g - off,
                                [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
+        } else if (SRC == MLP_SRC_GRID && tile_in_row(gp, tile)) {
+            const long long g0 = tile * MLP_TILE;
+            const int nx = gp.n[0];
+            tile_strip<DIM>(U, gp, (int)(g0 % nx), (int)((g0 / nx) % gp.n[1]),
+                            DIM == 3 ? (int)(g0 / ((long long)nx * gp.n[1])) : 0, tid, sQ);
+            __syncthreads();
+            strip_features<DIM>(sQ, tid, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
         } else if (g < gp.plane) {
             cell_features<DIM>(U, gp, g, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
         } else {
@@ -342,7 +399,8 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
 template <int DIM>
 constexpr int mlp_infer_smem()
 {
-    return (MLP_TILE * mlp_kpad(DIM) + MLP_H * mlp_kpad(DIM) + MLP_TILE * MLP_H + MLP_H * MLP_H) * 2;
+    return (MLP_TILE * mlp_kpad(DIM) + MLP_H * mlp_kpad(DIM) + MLP_TILE * MLP_H + MLP_H * MLP_H) * 2 +
+           (DIM == 3 ? 9 : 3) * (MLP_TILE + 2) * 5 * 4;
 }
 
 } // namespace mmf
