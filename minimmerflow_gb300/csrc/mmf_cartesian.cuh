@@ -311,16 +311,23 @@ __device__ __forceinline__ void march2d(const GridParams &gp, const StageArgs &s
         const double l = face_dir<A, 2>(abv, cur, 1, Fylo);
         if (out_col) lmax = max_nonneg(lmax, l);
     }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) Fyhi[k] = 0.0;
+    // unrolled so that the FP64 work of consecutive rows interleaves (the
+    // fast unit is built without implicit contraction, so the bits do not
+    // depend on the unrolling)
+#pragma unroll 4
     for (int y = y0; y < y1; ++y) {
         // x faces of row y (the cell's x pair opens the accumulator)
         const double lx = xfaces<A, 2>(cur, Fxlo, Fxhi);
         if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
         accumulate_pair<A, true>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
-        // row y+1 and the y face between y and y+1
+        // row y+1 and the y face between y and y+1 (output lanes only: the
+        // halo lanes only provide x-face states)
         load_record<A, STAGE, 2>(sa, gp, sc, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
-        const double ly = face_dir<A, 2>(cur, abv, 1, Fyhi);
-        if (STAGE <= STAGE_1 && out_col) lmax = max_nonneg(lmax, ly);
         if (out_col) {
+            const double ly = face_dir<A, 2>(cur, abv, 1, Fyhi);
+            if (STAGE <= STAGE_1) lmax = max_nonneg(lmax, ly);
             accumulate_pair<A, false>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
             store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * y, acc, cur.c);
         }
