@@ -43,13 +43,15 @@ FP64_OPS_PER_CELL_STAGE = None  # filled from the kernel model below (fast arith
 
 
 def fp64_ops_per_cell_update_2d():
-    """FP64 instructions per cell-update of the fast 2D kernel with zero
-    z-momentum (four stored fields), counted from the source per cell and stage:
-    record 29 (Newton reciprocal 4 + MUFU, velocities 2, rho|u|^2 2, p 2, a 9 with
-    MUFU, E+p 1, fluxes 5, wave speeds 2, status 0), faces 2 x 12, accumulation 12,
-    stage update (0, 8, 12) and the stage-2 state (4)  ->  65 + (0, 12, 12) per stage,
-    plus 1/16 for the two halo lanes of a warp."""
-    return int(round((3 * 65 + 24) * 32 / 30))
+    """Algorithmic FP64 instructions per cell-update of the fast 2D kernel with
+    zero z-momentum (four stored fields), counted from the source per cell and
+    stage: record 28 (reciprocal 3 + MUFU seed, velocities 2, rho|u|^2 2, p 2,
+    sound speed 9 with the MUFU seed, E+p 1, fluxes 5, wave speeds 2), two faces
+    2 x 12, accumulation 12, then the stage update (0, 8, 12) and the stage-2
+    input state (0, 4, 0): 64 + (0, 12, 12) per stage.  The halo lanes and halo
+    rows the kernel also evaluates are not counted (they are overhead, not
+    work of the algorithm)."""
+    return 3 * 64 + 24
 
 
 def read_peaks():
