@@ -70,19 +70,31 @@ private:
     int64_t m_n = 0;
 };
 
+/* The primitive state (p, u, v, w, T) behind the Dirichlet border faces of a
+ * problem (problem::getBorderBCInfo, src/problem.cpp:446-470): the
+ * forward-facing step's Mach 3 inflow; zero for the other problems, which
+ * have no Dirichlet faces. */
+inline std::array<double, 5> dirichletState(int problemType)
+{
+    std::array<double, 5> prim = {{0.0, 0.0, 0.0, 0.0, 0.0}};
+    if (problemType == MMF_FFSTEP) prim = {{1.0, 3.0, 0.0, 0.0, 1.0 / 1.4}};
+    return prim;
+}
+
 /* Recognises the uniform Cartesian grid behind a MeshGeometricalInfo (all
  * cells of one size h on a full nx x ny (x nz) lattice) and the border
  * condition of each side from the interface BC storage. */
 template <class MeshInfo, class InterfaceStorageInt>
 mmf_grid describeGrid(const MeshInfo &meshInfo, const InterfaceStorageInt &interfaceBCs, int order, int arith,
-                      std::vector<int64_t> *rawToCell)
+                      std::vector<int64_t> *rawToCell, int problemType = -1)
 {
     mmf_grid g;
     g.dim = meshInfo.getDimension();
     g.order = order;
     g.arith = arith;
     g.chunk = 0;
-    for (int k = 0; k < 5; ++k) g.dirichlet_prim[k] = 0.0;
+    const std::array<double, 5> dp = dirichletState(problemType);
+    for (int k = 0; k < 5; ++k) g.dirichlet_prim[k] = dp[k];
     const std::vector<std::size_t> &cells = meshInfo.getCellRawIds();
     if (cells.empty()) throw std::runtime_error("mmf_gb300: empty mesh");
     double h = meshInfo.rawGetCellSize(cells[0]);
@@ -140,14 +152,14 @@ std::map<const void *, std::unique_ptr<Context>> &contexts()
 /* The context of a mesh, created on first use and kept for later calls. */
 template <class MeshInfo, class InterfaceStorageInt>
 Context &contextFor(const MeshInfo &meshInfo, const InterfaceStorageInt &interfaceBCs, int order,
-                    int arith = MMF_ARITH_REFERENCE)
+                    int arith = MMF_ARITH_REFERENCE, int problemType = -1)
 {
     auto &m = detail::contexts<MeshInfo>();
     const void *key = &meshInfo;
     auto it = m.find(key);
     if (it == m.end()) {
         std::vector<int64_t> rawToCell;
-        mmf_grid g = describeGrid(meshInfo, interfaceBCs, order, arith, &rawToCell);
+        mmf_grid g = describeGrid(meshInfo, interfaceBCs, order, arith, &rawToCell, problemType);
         it = m.emplace(key, std::unique_ptr<Context>(new Context(g, rawToCell))).first;
     }
     return *it->second;
@@ -167,7 +179,7 @@ class UContext {
 public:
     template <class MeshInfo, class CellStorageBool, class InterfaceStorageInt>
     UContext(const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, const InterfaceStorageInt &interfaceBCs,
-             int arith, int device = 0)
+             int arith, int problemType = -1, int device = 0)
     {
         const std::vector<std::size_t> &cells = meshInfo.getCellRawIds();
         std::size_t n = 0;
@@ -205,7 +217,8 @@ public:
         d.area = area.data();
         d.normal = normal.data();
         d.bc = bc.data();
-        for (int k = 0; k < 5; ++k) d.dirichlet_prim[k] = 0.0;
+        const std::array<double, 5> dp = dirichletState(problemType);
+        for (int k = 0; k < 5; ++k) d.dirichlet_prim[k] = dp[k];
         d.arith = arith;
         check(mmf_umesh_create(&d, device, &m_u));
         m_n = (int64_t)n;
@@ -274,7 +287,7 @@ namespace euler {
  * border conditions) on the face-list kernels.  Both use the reference
  * arithmetic: the result equals the reference's bit for bit. */
 template <class ProblemType, class MeshInfo, class CellStorageBool, class CellStorageDouble, class InterfaceStorageInt>
-void computeRHS(ProblemType, const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, int order,
+void computeRHS(ProblemType problemType, const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, int order,
                 const CellStorageDouble &cellConservatives, const InterfaceStorageInt &interfaceBCs,
                 CellStorageDouble *cellsRHS, double *maxEig)
 {
@@ -284,13 +297,14 @@ void computeRHS(ProblemType, const MeshInfo &meshInfo, const CellStorageBool &ce
     if (uit == um.end() && detail::contexts<MeshInfo>().count(&meshInfo) == 0 &&
         !detail::cartesian_applies(meshInfo, cellSolvedFlag, interfaceBCs))
         uit = um.emplace(&meshInfo, std::unique_ptr<UContext>(new UContext(meshInfo, cellSolvedFlag, interfaceBCs,
-                                                                           MMF_ARITH_REFERENCE))).first;
+                                                                           MMF_ARITH_REFERENCE, (int)problemType)))
+                  .first;
     if (uit != um.end()) {
         check(mmf_umesh_compute_rhs(uit->second->get(), cellConservatives.rawData(0), cellsRHS->rawData(0), maxEig,
                                     uit->second->nCells()));
         return;
     }
-    Context &ctx = contextFor(meshInfo, interfaceBCs, order);
+    Context &ctx = contextFor(meshInfo, interfaceBCs, order, MMF_ARITH_REFERENCE, (int)problemType);
     check(mmf_compute_rhs(ctx.get(), cellConservatives.rawData(0), cellsRHS->rawData(0), maxEig, ctx.nCells()));
 }
 
@@ -309,30 +323,59 @@ inline void primitive2conservative(const double *p, double *c) { check(mmf_prim2
 }
 
 /* The SSP-RK3 loop of src/main.cpp:377-506 kept on the device: upload the
- * state once, advance, download when the host needs it. */
+ * state once, advance, download when the host needs it.  A full uniform grid
+ * with every cell solved runs on the Cartesian kernels; with the solved flags
+ * given, any other mesh (immersed bodies, refined meshes, mixed border
+ * conditions) runs on the face-list kernels, unsolved cells keeping their
+ * state as in the reference. */
 class Stepper {
 public:
     template <class MeshInfo, class InterfaceStorageInt>
-    Stepper(const MeshInfo &meshInfo, const InterfaceStorageInt &interfaceBCs, int arith = MMF_ARITH_FAST)
+    Stepper(const MeshInfo &meshInfo, const InterfaceStorageInt &interfaceBCs, int arith = MMF_ARITH_FAST,
+            int problemType = -1)
     {
         std::vector<int64_t> rawToCell;
-        mmf_grid g = describeGrid(meshInfo, interfaceBCs, 1, arith, &rawToCell);
+        mmf_grid g = describeGrid(meshInfo, interfaceBCs, 1, arith, &rawToCell, problemType);
         m_ctx.reset(new Context(g, rawToCell));
     }
+    template <class MeshInfo, class CellStorageBool, class InterfaceStorageInt>
+    Stepper(const MeshInfo &meshInfo, const CellStorageBool &cellSolvedFlag, const InterfaceStorageInt &interfaceBCs,
+            int arith, int problemType)
+    {
+        if (detail::cartesian_applies(meshInfo, cellSolvedFlag, interfaceBCs)) {
+            std::vector<int64_t> rawToCell;
+            mmf_grid g = describeGrid(meshInfo, interfaceBCs, 1, arith, &rawToCell, problemType);
+            m_ctx.reset(new Context(g, rawToCell));
+        } else {
+            m_uctx.reset(new UContext(meshInfo, cellSolvedFlag, interfaceBCs, arith, problemType));
+        }
+    }
+    /* true when the face-list kernels run this mesh */
+    bool faceList() const { return m_uctx != nullptr; }
     template <class CellStorageDouble>
-    void upload(const CellStorageDouble &U) { check(mmf_upload_state(m_ctx->get(), U.rawData(0), m_ctx->nCells())); }
+    void upload(const CellStorageDouble &U)
+    {
+        if (m_uctx) check(mmf_umesh_upload(m_uctx->get(), U.rawData(0), m_uctx->nCells()));
+        else check(mmf_upload_state(m_ctx->get(), U.rawData(0), m_ctx->nCells()));
+    }
     template <class CellStorageDouble>
-    void download(CellStorageDouble *U) { check(mmf_download_state(m_ctx->get(), U->rawData(0), m_ctx->nCells())); }
+    void download(CellStorageDouble *U)
+    {
+        if (m_uctx) check(mmf_umesh_download(m_uctx->get(), U->rawData(0), m_uctx->nCells()));
+        else check(mmf_download_state(m_ctx->get(), U->rawData(0), m_ctx->nCells()));
+    }
     void setTime(double cfl, double t, double tMax, int64_t maxSteps = -1)
     {
-        check(mmf_time_setup(m_ctx->get(), cfl, t, tMax, maxSteps));
+        if (m_uctx) check(mmf_umesh_time_setup(m_uctx->get(), cfl, t, tMax, maxSteps));
+        else check(mmf_time_setup(m_ctx->get(), cfl, t, tMax, maxSteps));
     }
     /* runs until tMax (or maxSteps); returns the number of steps */
     int64_t run(double *t, int64_t batch = 4096)
     {
         int64_t total = 0, done = 0;
         do {
-            check(mmf_advance(m_ctx->get(), batch, t, &done));
+            if (m_uctx) check(mmf_umesh_advance(m_uctx->get(), batch, t, &done));
+            else check(mmf_advance(m_ctx->get(), batch, t, &done));
             total += done;
         } while (done == batch);
         return total;
@@ -340,6 +383,7 @@ public:
 
 private:
     std::unique_ptr<Context> m_ctx;
+    std::unique_ptr<UContext> m_uctx;
 };
 
 } // namespace mmf_gb300

@@ -6,10 +6,13 @@
  * (test infrastructure); a small MeshGeometricalInfo-like class provides the
  * accessors the adapter reads.  Initial states come from the C oracle.
  *
- * usage: test_dropin <radsod|vortex_xy> <dim> <nCells> <steps> <out_loop.bin> <out_stepper.bin> [body]
+ * usage: test_dropin <radsod|vortex_xy|ffstep> <dim> <nCells> <steps> <out_loop.bin> <out_stepper.bin> [body]
  * 'body' makes the cells whose centroid lies in [1, 2.5] x [-1.5, 1.5] (x
  * [-10, 10]) solid and their fluid faces walls (main.cpp:222-277); the
- * adapter then runs on the face-list kernels.
+ * adapter then runs on the face-list kernels.  'ffstep' is the Mach 3
+ * forward-facing step on [0, 3.2]^2: the step [0.6, 4] x [-1, 0.2] is solid,
+ * the left border is the Dirichlet inflow, the right one free flow and the
+ * others reflecting (problem.cpp:404-432).
  */
 #include "bitpit_voloctree.hpp"
 #include "minimmerflow_gb300.hpp"
@@ -62,13 +65,15 @@ private:
 int main(int argc, char **argv)
 {
     if (argc < 7) return 2;
-    const int problem = std::strcmp(argv[1], "radsod") == 0 ? ORC_RADSOD : ORC_VORTEX_XY;
+    const int problem = std::strcmp(argv[1], "radsod") == 0   ? ORC_RADSOD
+                        : std::strcmp(argv[1], "ffstep") == 0 ? ORC_FFSTEP
+                                                              : ORC_VORTEX_XY;
     const int dim = std::atoi(argv[2]);
     const long n = std::atol(argv[3]);
     const int steps = std::atoi(argv[4]);
-    std::array<double, 3> origin = (problem == ORC_RADSOD) ? std::array<double, 3>{{0., 0., 0.}}
-                                                           : std::array<double, 3>{{-5., -5., -5.}};
-    const double length = (problem == ORC_RADSOD) ? 8.0 : 10.0;
+    std::array<double, 3> origin = (problem == ORC_VORTEX_XY) ? std::array<double, 3>{{-5., -5., -5.}}
+                                                              : std::array<double, 3>{{0., 0., 0.}};
+    const double length = (problem == ORC_RADSOD) ? 8.0 : (problem == ORC_FFSTEP) ? 3.2 : 10.0;
     const double cfl = 0.45;
     VolOctree mesh(dim, origin, length, length / n);
     MeshInfoLike meshInfo(mesh);
@@ -80,13 +85,25 @@ int main(int argc, char **argv)
     const bool body = argc > 7 && std::strcmp(argv[7], "body") == 0;
     for (std::size_t r = 0; r < nCells; ++r) {
         const std::array<double, 3> &c = meshInfo.rawGetCellCentroid(r);
-        const bool solid = body && c[0] > 1.0 && c[0] < 2.5 && c[1] > -1.5 && c[1] < 1.5;
+        bool solid = false;
+        if (body && problem == ORC_FFSTEP) solid = c[0] >= 0.6 && c[0] <= 4.0 && c[1] >= -1.0 && c[1] <= 0.2;
+        else if (body) solid = c[0] > 1.0 && c[0] < 2.5 && c[1] > -1.5 && c[1] < 1.5;
         solved.rawSet(r, !solid);
     }
     for (std::size_t f : meshInfo.getInterfaceRawIds()) {
         const Interface &itf = mesh.getInterfaces().rawAt(f);
-        if (itf.isBorder()) bcs[(long)f] = (problem == ORC_RADSOD ? MMF_BC_REFLECTING : MMF_BC_FREE_FLOW);
-        else bcs[(long)f] = (solved.rawAt(itf.getOwner()) != solved.rawAt(itf.getNeigh())) ? MMF_BC_WALL : MMF_BC_NONE;
+        if (itf.isBorder()) {
+            int bc = (problem == ORC_RADSOD ? MMF_BC_REFLECTING : MMF_BC_FREE_FLOW);
+            if (problem == ORC_FFSTEP) {
+                // problem.cpp:422-432 on the face centroid (owner centroid + h/2 along the normal)
+                const double x = meshInfo.rawGetCellCentroid((std::size_t)itf.getOwner())[0] +
+                                 0.5 * meshInfo.rawGetCellSize(0) * meshInfo.rawGetInterfaceNormal(f)[0];
+                bc = x < 1e-10 ? MMF_BC_DIRICHLET : (x > 3.2 - 1e-10 ? MMF_BC_FREE_FLOW : MMF_BC_REFLECTING);
+            }
+            bcs[(long)f] = bc;
+        } else {
+            bcs[(long)f] = (solved.rawAt(itf.getOwner()) != solved.rawAt(itf.getNeigh())) ? MMF_BC_WALL : MMF_BC_NONE;
+        }
     }
     orc_params prm;
     orc_params_default(&prm);
@@ -123,17 +140,9 @@ int main(int argc, char **argv)
     std::fwrite(U.rawData(0), sizeof(double), 5 * nCells, fp);
     std::fclose(fp);
 
-    if (body) {
-        // the face-list path has no Stepper in this adapter: write the loop result twice
-        fp = std::fopen(argv[6], "wb");
-        std::fwrite(U.rawData(0), sizeof(double), 5 * nCells, fp);
-        std::fclose(fp);
-        std::printf("steps %d %d t %.17g %.17g\n", steps, steps, t, t);
-        mmf_gb300::releaseContexts(meshInfo);
-        return 0;
-    }
-    // the same run kept on the device
-    mmf_gb300::Stepper stepper(meshInfo, bcs, MMF_ARITH_REFERENCE);
+    // the same run kept on the device (face-list kernels when a body is present)
+    mmf_gb300::Stepper stepper(meshInfo, solved, bcs, MMF_ARITH_REFERENCE, problem);
+    if (stepper.faceList() != body) return 3;
     stepper.upload(U0);
     stepper.setTime(cfl, 0.0, INFINITY, steps);
     double t2 = 0.0;

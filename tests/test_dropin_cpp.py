@@ -32,7 +32,7 @@ def test_dropin_builds(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("problem,dim,n,steps,body", [("radsod", 2, 64, 12, False), ("vortex_xy", 3, 16, 6, False),
-                                                      ("vortex_xy", 2, 64, 20, True)])
+                                                      ("vortex_xy", 2, 64, 20, True), ("ffstep", 2, 64, 40, True)])
 def test_dropin_loop_matches_oracle(orc, tmp_path, problem, dim, n, steps, body):
     exe = build_dropin(tmp_path)
     a, b = str(tmp_path / "loop.bin"), str(tmp_path / "stepper.bin")
@@ -40,9 +40,11 @@ def test_dropin_loop_matches_oracle(orc, tmp_path, problem, dim, n, steps, body)
     out = subprocess.check_output(cmd, timeout=300).decode()
     assert out.startswith("steps")
     prob = orc.PROBLEMS[problem]
-    origin, length = orc.reference_domain(prob)
+    origin, length = ((0.0, 0.0, 0.0), 3.2) if prob == orc.FFSTEP else orc.reference_domain(prob)
     m = orc.OracleMesh(prob, dim, (n, n, n if dim == 3 else 1), origin, length)
-    if body:
+    if body and prob == orc.FFSTEP:
+        m.set_bodies([((0.6, -1.0, -10), (4.0, 0.2, 10))])
+    elif body:
         m.set_bodies([((1.0, -1.5, -10), (2.5, 1.5, 10))])
     U_ref, t, s = m.run(m.initial_state(), 0.45, max_steps=steps)
     assert np.array_equal(np.fromfile(a).reshape(-1, 5), U_ref)
