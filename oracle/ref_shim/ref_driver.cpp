@@ -7,7 +7,7 @@
  * reconstruction::, euler:: and problem:: functions.
  *
  * usage: mmf_ref <problem> <dim> <nCells> <order> <CFL> <t_end|-|inf> [max_steps] [dump.bin]
- *               [length=L] [body=xmin,ymin,zmin,xmax,ymax,zmax ...]
+ *               [length=L] [body=xmin,ymin,zmin,xmax,ymax,zmax ...] [init=initial.bin]
  *   '-' takes the problem's default end time (problem.cpp:175-211); 'inf'
  *   runs exactly max_steps steps.  length= sets problem.domain.length (the
  *   forward-facing step has no default); each body= adds a box body to the
@@ -50,11 +50,14 @@ int main(int argc, char *argv[])
     // positional [max_steps] [dump], then key=value options
     std::vector<const char *> positional;
     int nBodies = 0;
+    const char *initDump = nullptr;
     for (int a = 7; a < argc; ++a) {
         const char *eq = std::strchr(argv[a], '=');
         if (!eq) { positional.push_back(argv[a]); continue; }
         const std::string key(argv[a], eq - argv[a]);
-        if (key == "length") {
+        if (key == "init") {
+            initDump = eq + 1;
+        } else if (key == "length") {
             config::root["problem"]["domain"].set("length", eq + 1);
         } else if (key == "body") {
             double b[6];
@@ -133,6 +136,13 @@ int main(int argc, char *argv[])
         const std::size_t cellRawId = cellRawIds[i];
         const Cell &cell = mesh.getCells().rawAt(cellRawId);
         problem::evalCellInitalConservatives(problemType, cell, meshInfo, cellConservatives.rawData(cellRawId));
+    }
+
+    if (initDump) {
+        FILE *fp = std::fopen(initDump, "wb");
+        if (!fp) return 3;
+        std::fwrite(cellConservatives.rawData(0), sizeof(double), nCells * N_FIELDS, fp);
+        std::fclose(fp);
     }
 
     double minCellSize = std::numeric_limits<double>::max();

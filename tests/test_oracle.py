@@ -158,3 +158,33 @@ def test_oracle_bodies_match_reference_build(orc, tmp_path, case):
     U, t, s = m.run(m.initial_state(), 0.45, max_steps=steps)
     assert s == steps
     assert np.array_equal(np.fromfile(dump).reshape(-1, 5), U)
+
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_FILES = sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+
+
+def golden_fixture_mesh(orc, g):
+    """The oracle mesh of a fixture written by tests/golden/make_golden.py."""
+    prob = orc.PROBLEMS[str(g["problem"])]
+    dim, n = int(g["dim"]), int(g["n"])
+    origin, length = ((0.0, 0.0, 0.0), float(g["length"])) if prob == orc.FFSTEP else orc.reference_domain(prob)
+    m = orc.OracleMesh(prob, dim, (n, n, n if dim == 3 else 1), origin, length)
+    b = g["body"]
+    if b.size:
+        m.set_bodies([(tuple(b[:3]), tuple(b[3:]))])
+    return m
+
+
+@pytest.mark.parametrize("name", GOLDEN_FILES)
+def test_oracle_reproduces_reference_fixtures(orc, name):
+    """The oracle against the reference's own outputs (fixtures made by the
+    reference build): initial state, final state and final time bit for bit,
+    and the final-error line of the reference driver."""
+    g = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    m = golden_fixture_mesh(orc, g)
+    assert np.array_equal(m.initial_state(), g["U0"])
+    U, t, steps = m.run(g["U0"], float(g["cfl"]), max_steps=int(g["steps"]))
+    assert steps == int(g["steps"]) and t == float(g["t"])
+    assert np.array_equal(U, g["U"])
+    assert "%.12e" % m.l1_density_error(U, t) == str(g["final_error"])
