@@ -577,9 +577,10 @@ def main():
         if rank != 0:
             return
         procs = args.cpu_procs or os.cpu_count() or 1
-        # each 'step' of the reference arm is a bounded sample of the workload
-        per = max(2.0, min(args.cpu_seconds, 60.0 / max(1, args.steps + args.warmup)))
-        base = cpu_baseline(args.n, per * max(1, args.steps), procs)
+        # a bounded sample of the workload: every core runs oracle steps of its
+        # own replica for 10-90 s of wall time in total, whatever K is
+        seconds = min(90.0, max(10.0, 2.0 * max(1, args.steps)))
+        base = cpu_baseline(args.n, seconds, procs)
         line = {"metric": metric, "value": base["value"], "unit": metric, "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * args.n * args.n / base["value"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
