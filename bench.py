@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -79,8 +80,7 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
-                                 ".bench_clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "mmf_bench_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
