@@ -5,7 +5,8 @@
  * algorithm (optimad/minimmerflow src/utils.cpp, src/euler.cpp,
  * src/reconstruction.cpp, src/problem.cpp and the time loop of src/main.cpp).
  * Only the test suite, the smoke check and the CPU-baseline leg of the
- * benchmark may load it, and only as the checker or the timed CPU baseline.
+ * benchmark may load it, and only as the reference results the GPU path is
+ * compared with, or as the timed CPU baseline.
  * The product path (minimmerflow_gb300) never calls into it.
  *
  * Parity is pinned: the five reference regression goldens

@@ -8,7 +8,7 @@
  * PatchKernel with a uniform Cartesian "octree", PatchInfo, config, log.
  *
  * TEST INFRASTRUCTURE: used only to compile the reference sources into
- * oracle/_ref as a checker for the C oracle.
+ * oracle/_ref, against which the C oracle is compared.
  */
 #ifndef MMF_SHIM_BITPIT_CONTAINERS_HPP
 #define MMF_SHIM_BITPIT_CONTAINERS_HPP

@@ -1,7 +1,7 @@
 /*
  * Driver for the reference numerics compiled against the bitpit stand-in
- * (TEST INFRASTRUCTURE: builds oracle/_ref/mmf_ref, the checker of the C
- * oracle).  It restates the setup and the SSP-RK3 loop of the reference
+ * (TEST INFRASTRUCTURE: builds oracle/_ref/mmf_ref, against which the C
+ * oracle is compared).  It restates the setup and the SSP-RK3 loop of the reference
  * src/main.cpp:197-506 and the error check of src/main.cpp:550-572 without
  * VTK output and MPI; all physics calls go to the reference's own
  * reconstruction::, euler:: and problem:: functions.
