@@ -354,14 +354,17 @@ __device__ __forceinline__ void march2d_o2(const GridParams &gp, const StageArgs
         const double l = side_face<A>(abv.r[1][1], cur.r[1][0], Fylo);
         if (out_col) lmax = max_nonneg(lmax, l);
     }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) Fyhi[k] = 0.0;
+#pragma unroll 4
     for (int y = y0; y < y1; ++y) {
         const double lx = xfaces_o2<A>(cur.r[0][1], cur.r[0][0], Fxlo, Fxhi);
         if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
         accumulate_pair<A, true>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
         load_sides<A, 2>(gp, state, S, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
-        const double ly = side_face<A>(cur.r[1][1], abv.r[1][0], Fyhi);
-        if (STAGE <= STAGE_1 && out_col) lmax = max_nonneg(lmax, ly);
-        if (out_col) {
+        if (out_col) {   // the halo lanes only provide x-face states
+            const double ly = side_face<A>(cur.r[1][1], abv.r[1][0], Fyhi);
+            if (STAGE <= STAGE_1) lmax = max_nonneg(lmax, ly);
             accumulate_pair<A, false>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
             store_output_o2<A, STAGE>(sa, gp, sc, state, (long long)x + (long long)nx * y, acc);
         }
