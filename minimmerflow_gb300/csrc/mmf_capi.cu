@@ -664,6 +664,8 @@ void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
 // stage-3 bands run in order on one stream so that the first downloads start
 // early.  Band launches use shorter marching chunks so that each has work for
 // every SM.
+static constexpr int S3_STREAMS = 2;   // streams the stage-3 bands take in turn
+
 struct BandPlan {
     int K = 0;
     int rows = 0;          // rows (planes) per band, a multiple of chunk
@@ -682,7 +684,7 @@ static BandPlan band_plan(const mmf_ctx *c)
     int K = 8;
     int rows = (p.n_slow + K - 1) / K;
     int ch;
-    if (gp.dim == 2) ch = (int)std::min<long long>(32, std::max<long long>(4, (long long)gp.nseg * rows / 2432));
+    if (gp.dim == 2) ch = std::min(8, rows);   // measured best for 1024^2 and 2048^2 with eight bands
     else ch = (int)std::min<long long>(32, std::max<long long>(2, (long long)gp.nseg * gp.nrowblk * rows / 304));
     rows = (rows + ch - 1) / ch * ch;
     p.K = (p.n_slow + rows - 1) / rows;
@@ -811,19 +813,25 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             continue;
         }
         // last step: stage 3, transposition and download, band by band, in
-        // band order on the compute stream so that the downloads start early
+        // band order on S3_STREAMS streams taken in turn (so that a band's
+        // launch overlaps the end of the previous one while the early bands
+        // still finish first and their downloads start early)
+        MMF_CUDA(cudaEventRecord(c->ev_s2, c->stream));
         for (int b = 0; b < p.K; ++b) {
             long long base, count;
             band_cells(b, base, count);
-            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U, c->stream));
-            soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, c->stream>>>(c->U, c->aos, base, count, plane);
+            cudaStream_t bs = c->band_stream[b % S3_STREAMS];
+            if (b < S3_STREAMS) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2, 0));
+            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U, bs));
+            soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, bs>>>(c->U, c->aos, base, count, plane);
             ++c->launches;
             MMF_CUDA(cudaPeekAtLastError());
-            MMF_CUDA(cudaEventRecord(c->ev_dn[b], c->stream));
+            MMF_CUDA(cudaEventRecord(c->ev_dn[b], bs));
             MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_dn[b], 0));
             MMF_CUDA(cudaMemcpyAsync(aos + NF * base, c->aos + NF * base, sizeof(double) * NF * count,
                                      cudaMemcpyDeviceToHost, c->copy_stream));
         }
+        for (int b = 0; b < p.K; ++b) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_dn[b], 0));
     }
     MMF_CUDA(cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
     MMF_CUDA(cudaStreamSynchronize(c->stream));
