@@ -661,9 +661,10 @@ void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
 // step's dt, a max over every cell of stage 1, so it runs on the whole grid.
 // The stage-1 band kernels run on one stream per band (band 0 at the highest
 // priority) so that they overlap one another and the transpositions; the
-// stage-3 bands run in order on one stream so that the first downloads start
-// early.  Band launches use shorter marching chunks so that each has work for
-// every SM.
+// stage-3 bands are issued in band order on two streams taken in turn, so that
+// a band's launch overlaps the end of the previous one while the first
+// downloads still start early.  Band launches march short chunks so that
+// each has work for every SM.
 static constexpr int S3_STREAMS = 2;   // streams the stage-3 bands take in turn
 
 struct BandPlan {
