@@ -780,13 +780,36 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
         MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
         MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
     }
-    // stage 1 of band q once the bands on both sides of it are on the device
-    // (the transpositions run in band order, so the last one it needs suffices)
-    for (int q = 0; q < p.K; ++q) {
-        const int need = (q == 0 && periodic_slow) ? p.K - 1 : std::min(q + 1, p.K - 1);
-        MMF_CUDA(cudaStreamWaitEvent(c->band_stream[q], c->ev_tr[need], 0));
-        MMF_CUDA(c->stage_gp(STAGE_1, band_params(c, p, q, q == 0), c->U, c->R, c->band_stream[q]));
-        MMF_CUDA(cudaEventRecord(c->ev_s1[q], c->band_stream[q]));
+    // stage 1 chunk by chunk as soon as the rows it reads are on the device:
+    // once bands 0..b are transposed (rows below r_b), the chunks whose top
+    // neighbour row is below r_b run (on band b's stream); chunk 0 of a
+    // periodic slow axis reads the last row and waits for the last band
+    {
+        const int nch = (p.n_slow + p.chunk - 1) / p.chunk;
+        int next = periodic_slow ? 1 : 0;   // first chunk not yet launched
+        for (int b = 0; b < p.K; ++b) {
+            const int rb = std::min(p.n_slow, (b + 1) * p.rows);
+            int upto = (b == p.K - 1) ? nch : (rb - 1) / p.chunk;   // chunks [next, upto) are ready
+            const bool first0 = periodic_slow && b == p.K - 1;
+            MMF_CUDA(cudaStreamWaitEvent(c->band_stream[b], c->ev_tr[b], 0));
+            if (upto > next || first0) {
+                GridParams g = c->gp;
+                g.chunk = p.chunk;
+                g.bookkeep = (next == 0 || first0) ? 1 : 0;   // once per stage (idempotent for stage 1)
+                if (upto > next) {
+                    g.chunk0 = next;
+                    g.nchunk = upto - next;
+                    MMF_CUDA(c->stage_gp(STAGE_1, g, c->U, c->R, c->band_stream[b]));
+                    next = upto;
+                }
+                if (first0) {
+                    g.chunk0 = 0;
+                    g.nchunk = 1;
+                    MMF_CUDA(c->stage_gp(STAGE_1, g, c->U, c->R, c->band_stream[b]));
+                }
+            }
+            MMF_CUDA(cudaEventRecord(c->ev_s1[b], c->band_stream[b]));
+        }
     }
     for (int q = 0; q < p.K; ++q) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_s1[q], 0));
     if (check_w) {
