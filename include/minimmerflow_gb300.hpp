@@ -8,6 +8,9 @@
  *   mmf_gb300::utils::conservative2primitive / primitive2conservative
  *                                           <- utils::*                    (src/utils.hpp:34-35)
  *   mmf_gb300::euler::evalSplitting         <- euler::evalSplitting        (src/euler.hpp:37)
+ *   mmf_gb300::euler::evalFluxes            <- euler::evalFluxes           (src/euler.hpp:39)
+ *   mmf_gb300::euler::evalInterfaceBCValues <- euler::evalInterfaceBCValues (src/euler.hpp:45-48)
+ *   mmf_gb300::reconstruction::eval         <- reconstruction::eval        (src/reconstruction.hpp:44)
  *   mmf_gb300::Stepper                      <- the SSP-RK3 loop            (src/main.cpp:377-506)
  *
  * Header-only C++11.  The mesh and storage types are template parameters so
@@ -268,6 +271,17 @@ void releaseContexts(const MeshInfo &meshInfo)
 }
 
 namespace reconstruction {
+/* reconstruction::eval (src/reconstruction.cpp:67-79): the reconstructed
+ * state at a point of a cell.  Order 1 is the cell mean (eval_1,
+ * src/reconstruction.cpp:89-97); the reference stops for any other order, and
+ * so does this host helper (order 2 lives in the device kernels). */
+template <class MeshInfo>
+void eval(std::size_t, const MeshInfo &, int order, const std::array<double, 3> &, const double *means, double *values)
+{
+    if (order != 1) throw std::runtime_error("mmf_gb300: reconstruction::eval supports order 1");
+    for (int k = 0; k < 5; ++k) values[k] = means[k];
+}
+
 /* reconstruction::computePolynomials (src/reconstruction.cpp:47-55): order 1
  * needs no polynomial data. */
 template <class ProblemType, class MeshInfo, class CellStorageBool, class CellStorageDouble, class InterfaceStorageInt>
@@ -313,6 +327,24 @@ inline void evalSplitting(const double *conservativeL, const double *conservativ
                           std::array<double, 5> *fluxes, double *lambda)
 {
     check(mmf_eval_splitting(1, conservativeL, conservativeR, n.data(), fluxes->data(), lambda));
+}
+
+/* euler::evalFluxes (src/euler.cpp:83-113): the physical flux along n. */
+inline void evalFluxes(const double *conservative, const double *primitive, const std::array<double, 3> &n,
+                       std::array<double, 5> *fluxes)
+{
+    check(mmf_eval_fluxes(1, conservative, primitive, n.data(), fluxes->data()));
+}
+
+/* euler::evalInterfaceBCValues (src/euler.cpp:261-308): the ghost state
+ * behind a border face of the given condition (the point is not used by any
+ * condition of the reference; Dirichlet takes the problem's inflow state). */
+template <class ProblemType>
+void evalInterfaceBCValues(ProblemType problemType, int BCType, const std::array<double, 3> &,
+                           const std::array<double, 3> &normal, const double *conservative, double *conservative_BC)
+{
+    const std::array<double, 5> dp = dirichletState((int)problemType);
+    check(mmf_eval_bc_values(1, BCType, normal.data(), conservative, dp.data(), conservative_BC));
 }
 }
 

@@ -105,6 +105,28 @@ int main(int argc, char **argv)
             bcs[(long)f] = (solved.rawAt(itf.getOwner()) != solved.rawAt(itf.getNeigh())) ? MMF_BC_WALL : MMF_BC_NONE;
         }
     }
+    // the reference's point-wise entry points through the adapter against the oracle
+    {
+        const double c[5] = {1.1, 0.3, -0.2, 0.05, 2.7}, nrm3[3] = {0.6, -0.8, 0.0};
+        const std::array<double, 3> n3 = {{0.6, -0.8, 0.0}}, pt = {{0.0, 0.0, 0.0}};
+        double pr[5], pr_ref[5], f_ref[5], g_ref[5], g[5], v[5];
+        mmf_gb300::utils::conservative2primitive(c, pr);
+        orc_cons2prim(c, pr_ref);
+        std::array<double, 5> f;
+        mmf_gb300::euler::evalFluxes(c, pr, n3, &f);
+        orc_eval_fluxes(c, pr_ref, nrm3, f_ref);
+        for (int k = 0; k < 5; ++k)
+            if (pr[k] != pr_ref[k] || f[k] != f_ref[k]) return 4;
+        for (int bc : {MMF_BC_FREE_FLOW, MMF_BC_REFLECTING, MMF_BC_WALL, MMF_BC_DIRICHLET}) {
+            mmf_gb300::euler::evalInterfaceBCValues(ORC_FFSTEP, bc, pt, n3, c, g);
+            orc_eval_bc(ORC_FFSTEP, bc, pt.data(), nrm3, c, g_ref);
+            for (int k = 0; k < 5; ++k)
+                if (g[k] != g_ref[k]) return 5;
+        }
+        mmf_gb300::reconstruction::eval(0, meshInfo, 1, pt, c, v);
+        for (int k = 0; k < 5; ++k)
+            if (v[k] != c[k]) return 6;
+    }
     orc_params prm;
     orc_params_default(&prm);
     for (std::size_t r = 0; r < nCells; ++r)
