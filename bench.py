@@ -661,7 +661,8 @@ def main():
         workload = dict(workload, decomposition={"rows_per_chunk" if r["case"].dim == 2 else "planes_per_chunk":
                                                  r["tuned"][0], "warps_per_block": r["tuned"][1] or None,
                                                  "chosen_by": "mmf_autotune"})
-    fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock)
+    fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock, operands reused)
+    fp64_peak_mixed = 505.2e9   # measured DADD / DMUL / DFMA with varying operands (1.61 per SM per clock)
     line = {
         "metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
@@ -679,7 +680,11 @@ def main():
                  "achieved_ops_per_s": fp64_ops * r["value"] / world if fp64_ops else None,
                  "peak_ops_per_s": fp64_peak,
                  "frac": fp64_ops * r["value"] / world / fp64_peak if fp64_ops else None,
-                 "peak_source": "measured DFMA issue rate (probe), not in MEASURED_PEAKS.json"},
+                 "peak_source": "measured DFMA issue rate (probe), not in MEASURED_PEAKS.json",
+                 "peak_mixed_ops_per_s": fp64_peak_mixed,
+                 "frac_of_mixed": fp64_ops * r["value"] / world / fp64_peak_mixed if fp64_ops else None,
+                 "peak_mixed_source": ("measured rate of DADD, DMUL and DFMA whose operands change from one "
+                                       "instruction to the next (probe)")},
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],
         "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,
