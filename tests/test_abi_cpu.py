@@ -68,3 +68,28 @@ def test_no_cpu_fallback_without_gpu(mmf):
     with pytest.raises(mmf.capi.MMFError):
         from minimmerflow_gb300 import euler
         euler.conservative2primitive([[1.0, 0, 0, 0, 2.5]])
+
+
+def test_null_handles_are_argument_errors(mmf):
+    """Every entry point that takes a context, a batch, a face-list context or
+    an MLP rejects a null handle with MMF_ERR_ARG before touching a device."""
+    lib = mmf.capi.load()
+    d = C.c_double()
+    i64 = C.c_int64()
+    ci = C.c_int()
+    prob = mmf.capi.Problem()
+    calls = {
+        "mmf_upload_state": (None, None, 0), "mmf_download_state": (None, None, 0),
+        "mmf_compute_rhs": (None, None, None, None, 0), "mmf_time_setup": (None, 0.5, 0.0, 1.0, -1),
+        "mmf_advance": (None, 1, C.byref(d), C.byref(i64)), "mmf_advance_async": (None, 1),
+        "mmf_advance_host": (None, None, 0, 1, C.byref(d)), "mmf_rk_stage": (None, 1),
+        "mmf_autotune": (None, 2, C.byref(ci), C.byref(ci)),
+        "mmf_init_state": (None, C.byref(prob)), "mmf_l1_density_error": (None, C.byref(prob), 0.0, C.byref(d)),
+        "mmf_write_vtk": (None, b"x.vti"), "mmf_save_checkpoint": (None, b"x.ckpt"),
+        "mmf_load_checkpoint": (None, b"x.ckpt"),
+        "mmf_umesh_advance": (None, 1, C.byref(d), C.byref(i64)),
+        "mmf_batch_advance_async": (None, 1), "mmf_batch_synchronize": (None,),
+    }
+    for name, args in calls.items():
+        rc = getattr(lib, name)(*args)
+        assert rc == mmf.capi.MMF_ERR_ARG, (name, rc)
