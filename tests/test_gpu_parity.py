@@ -236,14 +236,15 @@ def test_vortex_3d_both_axes(orc, mmf, arith):
 
 
 def test_full_size_sod_symmetry_and_mass(mmf):
-    """1024^2 radial Sod, a few steps: the solution keeps the x<->y and mirror
-    symmetries of the initial state, and mass is conserved while the waves are
-    inside the domain."""
+    """The 1024^2 radial Sod of the benchmark, integrated to t = 0.25: the
+    solution keeps the x<->y and mirror symmetries of the initial state, and
+    mass is conserved (the shock, at r ~ 0.94, is still inside [-1, 1]^2)."""
     case = mmf.problem.radial_sod_2d(n=1024)
     U0 = case.initial_state()
     with case.solver(arith="fast") as s:
-        U, t, steps = s.run(U0, case.cfl, max_steps=20)
-    assert steps == 20
+        U, t, steps = s.run(U0, case.cfl, t_end=0.25)
+        assert s.status() == 0
+    assert t == 0.25 and steps > 300
     rho = U[:, 0].reshape(1024, 1024)
     np.testing.assert_allclose(rho, rho.T, rtol=1e-13, atol=0)
     np.testing.assert_allclose(rho, rho[::-1, :], rtol=1e-13, atol=0)
@@ -303,3 +304,27 @@ def test_autotune_keeps_state_and_bits(mmf, dim, order):
             outs.append((s.download(), t, steps))
     assert outs[0][1:] == outs[1][1:] and outs[0][2] == 9
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
+
+
+@pytest.mark.parametrize("axis", ["z", "x"])
+def test_full_size_vortex3d_is_invariant_along_its_axis(mmf, axis):
+    """The 256^3 periodic vortex of the benchmark, 50 steps: the initial state
+    does not depend on the coordinate along the vortex axis and the borders are
+    periodic, so every plane across the axis must stay bit for bit the same
+    (the axial faces contribute exactly zero).  The planes also match the 2D
+    vortex on 256^2 within the fast-arithmetic bound."""
+    P = mmf.problem
+    n = 256
+    case = P.vortex(3, n, axis=axis, steps=50)
+    with case.solver(arith="fast") as s:
+        U, t, steps = s.run(case.initial_state(), case.cfl, max_steps=50)
+    assert steps == 50
+    V = U.reshape(n, n, n, 5)                       # [z][y][x][field]
+    planes = V if axis == "z" else np.moveaxis(V, 2, 0)
+    assert all(np.array_equal(planes[0], planes[k]) for k in range(1, n))
+    if axis == "z":
+        c2 = P.vortex(2, n, steps=50)
+        with c2.solver(arith="fast") as s2:
+            U2, t2, _ = s2.run(c2.initial_state(), c2.cfl, max_steps=50)
+        assert abs(t2 - t) <= 1e-13 * t
+        assert rel_err(planes[0].reshape(-1, 5), U2) <= FAST_RTOL
