@@ -107,3 +107,26 @@ def test_batch_order2_with_indicator_equals_single_contexts(mmf):
             indicator.use_indicator(s, mlp, 0.5)
             U, t, n = s.run(U0, c.cfl, max_steps=6)
         assert np.array_equal(out[i], U), c.name
+
+
+def test_full_sweep_every_case_equals_its_own_context(mmf):
+    """The benchmark's sweep itself (512 cases, seed 20261203, sides 32..512):
+    after 10 steps in one batch, every case holds exactly the state of its own
+    single-case run."""
+    from minimmerflow_gb300.batch import BatchEuler
+    cases = mmf.problem.batched_sweep(ncases=512, seed=20261203)
+    states = [c.initial_state() for c in cases]
+    steps = 10
+    with BatchEuler(cases, arith="fast") as b:
+        b.upload(states)
+        b.time_setup(max_steps=steps)
+        b.autotune(trial_steps=2)
+        b.advance_async(steps)
+        b.synchronize()
+        out = b.unpack(b.download())
+        assert all(b.case_info(i)[2] == 0 for i in range(len(cases)))
+    for i, (c, U0) in enumerate(zip(cases, states)):
+        with c.solver(arith="fast") as s:
+            U, t, n = s.run(U0, c.cfl, max_steps=steps)
+        assert n == steps
+        assert np.array_equal(out[i], U), c.name
