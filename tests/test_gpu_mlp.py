@@ -191,3 +191,32 @@ def test_learned_limiter_on_sod_stays_physical(mmf):
         U_learn, _, _ = s.run(U0, case.cfl, max_steps=20)
         assert s.status() == 0
     assert np.abs(U_learn - U_plain).sum() < 2e-3 * np.abs(U_plain).sum()
+
+
+def test_shipped_indicator_gain_on_the_vortex_config(mmf):
+    """The shipped, trained 2D indicator on the 64^2 periodic vortex of the
+    reference's CPU-runnable configuration (order 2, CFL 0.5, 100 steps): most
+    cells skip the limiter, and the L1 density error against the exact
+    solution is no more than 1% above the fully limited run's -- the gain of
+    the network over the method without it is the limiter work it removes at
+    no loss of accuracy."""
+    from minimmerflow_gb300 import indicator, train_indicator
+    mlp, thr = train_indicator.load(2)
+    assert mlp is not None
+    case = mmf.problem.vortex(2, 64, steps=100)
+    U0 = case.initial_state()
+    with case.solver(arith="fast", order=2) as s:
+        U_plain, t, _ = s.run(U0, case.cfl, max_steps=100)
+        _, active = s.compute_polynomials(U0)
+        limited_plain = active.mean()
+    with case.solver(arith="fast", order=2) as s:
+        s.upload(U0)
+        _, flags = indicator.run_indicator(s, mlp, thr)
+        indicator.use_indicator(s, mlp, thr)
+        U_learn, t2, _ = s.run(U0, case.cfl, max_steps=100)
+        assert s.status() == 0
+    e_plain = case.l1_density_error(U_plain, t)
+    e_learn = case.l1_density_error(U_learn, t2)
+    print("flagged %.3f limited-by-MC %.3f e_plain %.6e e_learn %.6e" % (flags.mean(), limited_plain, e_plain, e_learn))
+    assert flags.mean() < 0.5                    # at least half the cells skip the limiter
+    assert e_learn <= 1.01 * e_plain
