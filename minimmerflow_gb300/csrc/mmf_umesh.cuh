@@ -217,11 +217,11 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
                 const long long code = m.csr_face[i];
                 const bool owner = code < 0;
                 const long long f = owner ? -code - 1 : code;
+                // acc -+ P (euler.cpp:237-247) as one fused operation with the
+                // sign as a factor: exact product, one rounding, the same bits
+                const double sg = owner ? -1.0 : 1.0;
 #pragma unroll
-                for (int k = 0; k < NF; ++k) {
-                    const double p = __ldg(P + k * nf + f);
-                    acc[k] = owner ? acc[k] - p : acc[k] + p;    // euler.cpp:237-247
-                }
+                for (int k = 0; k < NF; ++k) acc[k] = fma(sg, __ldg(P + k * nf + f), acc[k]);
             }
         }
         const double V = m.vol[c];
