@@ -596,21 +596,31 @@ int mmf_advance(mmf_ctx *c, int64_t n_steps, double *t_out, int64_t *steps_done)
     if (n_steps < 0) return fail(MMF_ERR_ARG, "n_steps < 0");
     if (!c->graph_many && (rc = build_graph(c, GRAPH_STEPS, &c->graph_many))) return rc;
     if (!c->graph_one && (rc = build_graph(c, 1, &c->graph_one))) return rc;
-    Ctrl before;
+    // The graphs are enqueued in rounds of at most CHECK_STEPS steps; after
+    // each round the control block tells whether the run has ended (end time,
+    // step limit or a non-physical state), so that asking for many more steps
+    // than the run needs launches no idle graphs.
+    constexpr int64_t CHECK_STEPS = 64 * GRAPH_STEPS;
+    Ctrl before, after;
     MMF_CUDA(cudaMemcpyAsync(&before, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
     int64_t left = n_steps;
-    while (left >= GRAPH_STEPS) {
-        MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
-        c->launches += c->launches_per_step() * GRAPH_STEPS;
-        left -= GRAPH_STEPS;
+    for (;;) {
+        int64_t round = left < CHECK_STEPS ? left : CHECK_STEPS;
+        left -= round;
+        while (round >= GRAPH_STEPS) {
+            MMF_CUDA(cudaGraphLaunch(c->graph_many, c->stream));
+            c->launches += c->launches_per_step() * GRAPH_STEPS;
+            round -= GRAPH_STEPS;
+        }
+        while (round-- > 0) {
+            MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
+            c->launches += c->launches_per_step();
+        }
+        MMF_CUDA(cudaMemcpyAsync(&after, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+        MMF_CUDA(cudaStreamSynchronize(c->stream));
+        const bool ended = !(after.t < after.t_end && after.step < after.max_steps) || after.status != 0;
+        if (left == 0 || ended) break;
     }
-    while (left-- > 0) {
-        MMF_CUDA(cudaGraphLaunch(c->graph_one, c->stream));
-        c->launches += c->launches_per_step();
-    }
-    Ctrl after;
-    MMF_CUDA(cudaMemcpyAsync(&after, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
-    MMF_CUDA(cudaStreamSynchronize(c->stream));
     if (t_out) *t_out = after.t;
     if (steps_done) *steps_done = after.step - before.step;
     if (after.status) return fail(MMF_ERR_STATE, "non-physical state (negative density/pressure or NaN)");

@@ -327,22 +327,30 @@ int mmf_umesh_advance(mmf_umesh *u, int64_t n_steps, double *t_out, int64_t *ste
     if (!u->time_ready) return set_last_error(MMF_ERR_ARG, "mmf_umesh_time_setup first");
     if (!u->g_many && (rc = um_graph(u, GRAPH_STEPS, &u->g_many))) return rc;
     if (!u->g_one && (rc = um_graph(u, 1, &u->g_one))) return rc;
+    // rounds of at most CHECK_STEPS steps, stopping once the run has ended
+    constexpr int64_t CHECK_STEPS = 64 * GRAPH_STEPS;
     Ctrl before, after;
     UM_CUDA(cudaMemcpyAsync(&before, u->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, u->stream));
     int64_t left = n_steps;
-    while (left >= GRAPH_STEPS) {
-        UM_CUDA(cudaGraphLaunch(u->g_many, u->stream));
-        u->launches += u->launches_per_step() * GRAPH_STEPS;
-        left -= GRAPH_STEPS;
+    for (;;) {
+        int64_t round = left < CHECK_STEPS ? left : CHECK_STEPS;
+        left -= round;
+        while (round >= GRAPH_STEPS) {
+            UM_CUDA(cudaGraphLaunch(u->g_many, u->stream));
+            u->launches += u->launches_per_step() * GRAPH_STEPS;
+            round -= GRAPH_STEPS;
+        }
+        while (round-- > 0) {
+            UM_CUDA(cudaGraphLaunch(u->g_one, u->stream));
+            u->launches += u->launches_per_step();
+        }
+        UM_CUDA(cudaMemcpyAsync(&after, u->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, u->stream));
+        UM_CUDA(cudaStreamSynchronize(u->stream));
+        if (left == 0 || !(after.t < after.t_end && after.step < after.max_steps) || after.status) break;
     }
-    while (left-- > 0) {
-        UM_CUDA(cudaGraphLaunch(u->g_one, u->stream));
-        u->launches += u->launches_per_step();
-    }
-    UM_CUDA(cudaMemcpyAsync(&after, u->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, u->stream));
-    UM_CUDA(cudaStreamSynchronize(u->stream));
     if (t_out) *t_out = after.t;
     if (steps_done) *steps_done = after.step - before.step;
+    if (after.status) return set_last_error(MMF_ERR_STATE, "non-physical state (negative density/pressure or NaN)");
     return MMF_OK;
 }
 

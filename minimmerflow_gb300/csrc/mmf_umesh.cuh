@@ -208,9 +208,21 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
         if (!sc.active) return;
     }
     const long long n = m.ncells, nf = m.nfaces;
+    unsigned status = 0;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
         double acc[NF] = {0., 0., 0., 0., 0.};
         const bool solved = m.solved[c] != 0;
+        if (STAGE == STAGE_1 && solved) {
+            // the stage input of a solved cell: rho < 0, p < 0 (2 rho E < |m|^2
+            // for rho > 0, division-free) or NaN, as the Cartesian kernels flag
+            // it (the reference only logs it, euler.cpp:93-101)
+            double u[NF];
+            uload(state, n, c, u);
+            const double m2 = fma(u[3], u[3], fma(u[2], u[2], u[1] * u[1]));
+            const double q = fma(2.0 * u[0], u[4], -m2);
+            status |= state_flags(u[0], u[0] > 0.0 ? q : 0.0);
+            if (q != q) status |= 4u;
+        }
         if (solved) {
             const long long e = m.csr_off[c + 1];
             for (long long i = m.csr_off[c]; i < e; ++i) {
@@ -242,6 +254,10 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
                                            : fma(2.0 / 3.0, fma(sc.dt / V, acc[k], w), u * (1.0 / 3.0));
             }
         }
+    }
+    if (STAGE == STAGE_1) {
+        status = __reduce_or_sync(0xffffffffu, status);
+        if ((threadIdx.x & 31) == 0 && status) atomicOr(&ctrl->status, status);
     }
 }
 

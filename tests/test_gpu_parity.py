@@ -328,3 +328,17 @@ def test_full_size_vortex3d_is_invariant_along_its_axis(mmf, axis):
             U2, t2, _ = s2.run(c2.initial_state(), c2.cfl, max_steps=50)
         assert abs(t2 - t) <= 1e-13 * t
         assert rel_err(planes[0].reshape(-1, 5), U2) <= FAST_RTOL
+
+
+def test_advance_stops_at_the_end_time(mmf):
+    """mmf_advance with many more steps than the run needs launches no idle
+    graphs: it returns promptly once t_end is reached."""
+    import time
+    case = mmf.problem.radial_sod_2d(64, t_end=0.05)
+    with case.solver() as s:
+        s.upload(case.initial_state())
+        s.time_setup(case.cfl, 0.0, 0.05)
+        t0 = time.perf_counter()
+        t, steps = s.advance(1 << 24)
+        assert time.perf_counter() - t0 < 5.0
+        assert t == 0.05 and steps > 0

@@ -69,3 +69,30 @@ def test_forward_facing_step(orc, mmf, arith):
         assert rel_err(U[~inside], U_ref[~inside]) <= FAST_RTOL
     # the step reflects the flow: a bow shock raises the density ahead of it
     assert U[~inside, 0].max() > 1.5 * U0[0, 0]
+
+
+def test_face_list_reports_negative_pressure(orc, mmf):
+    """A non-physical input state on the face-list path is reported as
+    MMF_ERR_STATE, not trapped (the Cartesian kernels do the same)."""
+    from minimmerflow_gb300.umesh import UnstructuredEuler
+    m = orc.OracleMesh(orc.RADSOD, 2, (16, 16, 1), (0, 0, 0), 8.0)
+    U0 = m.initial_state()
+    U0[37, 4] = -1.0
+    with UnstructuredEuler.from_oracle_mesh(m, arith="fast") as u:
+        with pytest.raises(mmf.capi.MMFError) as ei:
+            u.run(U0, 0.45, max_steps=2)
+        assert ei.value.code == mmf.capi.MMF_ERR_STATE
+
+
+def test_face_list_stops_at_the_end_time(orc, mmf):
+    """Asking for many more steps than the run needs returns promptly."""
+    import time
+    from minimmerflow_gb300.umesh import UnstructuredEuler
+    m = orc.OracleMesh(orc.RADSOD, 2, (16, 16, 1), (0, 0, 0), 8.0)
+    with UnstructuredEuler.from_oracle_mesh(m, arith="fast") as u:
+        u.upload(m.initial_state())
+        u.time_setup(0.45, 0.0, 0.05)
+        t0 = time.perf_counter()
+        t, steps = u.advance(1 << 24)
+        assert time.perf_counter() - t0 < 5.0
+        assert t == 0.05 and steps > 0
