@@ -576,7 +576,8 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        procs = args.cpu_procs or os.cpu_count() or 1
+        usable = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        procs = args.cpu_procs or usable
         # a bounded sample of the workload: every core runs oracle steps of its
         # own replica for 10-90 s of wall time in total, whatever K is
         seconds = min(90.0, max(10.0, 2.0 * max(1, args.steps)))
