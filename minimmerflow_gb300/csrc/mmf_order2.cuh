@@ -60,20 +60,47 @@ __device__ __forceinline__ double mc_slope(double a, double b, double central)
     }
 }
 
+// |x| as the bit pattern of a non-negative double (integer pipe); these
+// compare like the values they encode
+__device__ __forceinline__ long long abs_bits(double x)
+{
+    return __double_as_longlong(x) & 0x7fffffffffffffffll;
+}
+
+// Fast arithmetic: the MC slope with its compares, absolute values, minima
+// and sign on the integer pipe: a and b of opposite signs (or one of them
+// zero) -> 0; else sign(a) min(2 min(|a|, |b|), |central|), where the
+// doubling is exact.  Equal to mc_slope except when a b underflows to zero
+// with a and b of the same sign (|a|, |b| below 1e-154).
+__device__ __forceinline__ double mc_slope_bits(double a, double b, double central)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
+    if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;
+    const double m = __longlong_as_double(ma < mb ? ma : mb);
+    const long long m2 = __double_as_longlong(m + m), mc = abs_bits(central);
+    return __longlong_as_double((m2 < mc ? m2 : mc) | (ia & (long long)0x8000000000000000ull));
+}
+
 // division-free admissibility of a state: rho > 0 and 2 rho E > |m|^2
 template <class A>
 __device__ __forceinline__ bool admissible(const double *c)
 {
     constexpr int NV = A::NVAR;
-    if (!(c[0] > 0.0)) return false;
     if (IsExact<A>::value) {
+        if (!(c[0] > 0.0)) return false;
         double m2 = c[1] * c[1] + c[2] * c[2];
         if (NV == 5) m2 = m2 + c[3] * c[3];
         return (2.0 * c[0] * c[NV - 1] - m2) > 0.0;
     }
+    // fast: "x > 0" as 0 < bits(x) < bits(+inf) on the integer pipe (NaN fails, as in the compare)
+    const long long inf = 0x7ff0000000000000ll;
+    const long long ir = __double_as_longlong(c[0]);
+    if (!(ir > 0 && ir <= inf)) return false;
     double m2 = fma(c[2], c[2], c[1] * c[1]);
     if (NV == 5) m2 = fma(c[3], c[3], m2);
-    return fma(2.0 * c[0], c[NV - 1], -m2) > 0.0;
+    const long long iq = __double_as_longlong(fma(2.0 * c[0], c[NV - 1], -m2));
+    return iq > 0 && iq <= inf;
 }
 
 // reconstructed face state U + off sigma (off = +-1/2)
@@ -106,6 +133,8 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
     load_plain<A>(oa.state, n, g, uc);
     const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
     bool act = false;
+    // fast arithmetic: the activity threshold as the bit pattern of a non-negative double
+    const long long act_thr = IsExact<A>::value ? 0 : abs_bits(1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1])));
     double sig[DIM][NV];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -133,8 +162,13 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
             const double central = 0.5 * (a + b);
             double sl = central;
             if (limit) {
-                sl = mc_slope<A>(a, b, central);
-                if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
+                if (IsExact<A>::value) {
+                    sl = mc_slope<A>(a, b, central);
+                    if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
+                } else {
+                    sl = mc_slope_bits(a, b, central);
+                    act |= abs_bits(sl - central) > act_thr;
+                }
             }
             sig[d][k] = sl;
         }
