@@ -133,8 +133,9 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
     load_plain<A>(oa.state, n, g, uc);
     const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
     bool act = false;
+    const bool track = oa.active != nullptr;
     // fast arithmetic: the activity threshold as the bit pattern of a non-negative double
-    const long long act_thr = IsExact<A>::value ? 0 : abs_bits(1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1])));
+    const long long act_thr = (IsExact<A>::value || !track) ? 0 : abs_bits(1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1])));
     double sig[DIM][NV];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -162,12 +163,13 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
             const double central = 0.5 * (a + b);
             double sl = central;
             if (limit) {
+                // the activity is only recorded where a caller keeps it (stage 1)
                 if (IsExact<A>::value) {
                     sl = mc_slope<A>(a, b, central);
-                    if (fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
+                    if (track && fabs(sl - central) > 1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1]))) act = true;
                 } else {
                     sl = mc_slope_bits(a, b, central);
-                    act |= abs_bits(sl - central) > act_thr;
+                    if (track) act |= abs_bits(sl - central) > act_thr;
                 }
             }
             sig[d][k] = sl;
