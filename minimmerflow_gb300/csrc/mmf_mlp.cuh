@@ -57,6 +57,26 @@ __host__ __device__ __forceinline__ int core_offset(int row, int k, int rows)
     return (((k >> 3) * (rows >> 3) + (row >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
 }
 
+// Writes one row of a K-major BF16 operand (core-matrix layout) eight
+// elements at a time: put(k, v) for k = 0, 1, 2, ... in order; every full
+// group of eight (16 contiguous bytes of the row) goes out in one 16-byte
+// shared-memory store.  With the k loops unrolled the packing stays in
+// registers.
+struct RowPacker {
+    __nv_bfloat16 *base;
+    int row, rows;
+    uint32_t w[4];
+    __device__ __forceinline__ void put(int k, float v)
+    {
+        const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v));
+        const int j = (k & 7) >> 1;
+        if (k & 1) w[j] |= h << 16;
+        else w[j] = h;
+        if ((k & 7) == 7)
+            *reinterpret_cast<uint4 *>(base + core_offset(row, k - 7, rows)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+};
+
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x)
 {
@@ -312,6 +332,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
 
     for (long long tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
         const long long g = tile * MLP_TILE + tid;
+        RowPacker pk{sX, tid, MLP_TILE, {0u, 0u, 0u, 0u}};
         // features of this thread's cell -> BF16 operand rows
         if (g < gp.plane && SRC == MLP_SRC_X) {
             for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = X[g * KP + k];
@@ -319,18 +340,19 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
             const int c = case_of(bg, g);
             const long long off = bg.offsets[c];
             cell_features<DIM>(U + off, bg.cases[c].gp, g - off,
-                               [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
+                               [&](int k, float v) { pk.put(k, v); });
         } else if (SRC == MLP_SRC_GRID && tile_in_row(gp, tile)) {
             const long long g0 = tile * MLP_TILE;
             const int nx = gp.n[0];
             tile_strip<DIM>(U, gp, (int)(g0 % nx), (int)((g0 / nx) % gp.n[1]),
                             DIM == 3 ? (int)(g0 / ((long long)nx * gp.n[1])) : 0, tid, sQ);
             __syncthreads();
-            strip_features<DIM>(sQ, tid, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
+            strip_features<DIM>(sQ, tid, [&](int k, float v) { pk.put(k, v); });
         } else if (g < gp.plane) {
-            cell_features<DIM>(U, gp, g, [&](int k, float v) { sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(v); });
+            cell_features<DIM>(U, gp, g, [&](int k, float v) { pk.put(k, v); });
         } else {
-            for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = __float2bfloat16(0.0f);
+#pragma unroll
+            for (int k = 0; k < KP; ++k) pk.put(k, 0.0f);
         }
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -350,12 +372,13 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (!__syncthreads_and(ok)) { if (tid == 0) { atomicExch(err, 1); s_fail = 1; } break; }
         // h1 = GELU(z1 + b1) -> BF16 operand of layer 2
+        RowPacker ph{sH, tid, MLP_TILE, {0u, 0u, 0u, 0u}};
 #pragma unroll
         for (int c0 = 0; c0 < MLP_H; c0 += 16) {
             float v[16];
             tmem_ld16(tmem + lane_addr + (uint32_t)c0, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) sH[core_offset(tid, c0 + j, MLP_TILE)] = __float2bfloat16(gelu(v[j] + s_b1[c0 + j]));
+            for (int j = 0; j < 16; ++j) ph.put(c0 + j, gelu(v[j] + s_b1[c0 + j]));
         }
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
