@@ -209,6 +209,10 @@ int mmf_destroy(mmf_ctx *c)
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
     }
+    if (c->tr_stream) {
+        cudaStreamSynchronize(c->tr_stream);
+        cudaStreamDestroy(c->tr_stream);
+    }
     for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
         if (c->band_stream[b]) { cudaStreamSynchronize(c->band_stream[b]); cudaStreamDestroy(c->band_stream[b]); }
         cudaEvent_t evs[4] = {c->ev_up[b], c->ev_tr[b], c->ev_s1[b], c->ev_dn[b]};
@@ -696,7 +700,7 @@ static BandPlan band_plan(const mmf_ctx *c)
     int rows = (p.n_slow + K - 1) / K;
     int ch;
     if (gp.dim == 2) ch = std::min(8, rows);   // measured best for 1024^2 and 2048^2 with eight bands
-    else ch = (int)std::min<long long>(32, std::max<long long>(2, (long long)gp.nseg * gp.nrowblk * rows / 304));
+    else ch = std::min(16, rows);                // measured best for 256^3 (16 against 8, 18 and 32)
     rows = (rows + ch - 1) / ch * ch;
     p.K = (p.n_slow + rows - 1) / rows;
     p.rows = rows;
@@ -721,6 +725,7 @@ static int pipeline_resources(mmf_ctx *c)
     int least = 0, greatest = 0;
     MMF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     MMF_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    MMF_CUDA(cudaStreamCreateWithPriority(&c->tr_stream, cudaStreamNonBlocking, greatest));
     for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
         const int prio = std::min(least, greatest + b);   // greatest is the numerically lowest
         MMF_CUDA(cudaStreamCreateWithPriority(&c->band_stream[b], cudaStreamNonBlocking, prio));
@@ -768,6 +773,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     MMF_CUDA(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
     MMF_CUDA(cudaEventRecord(c->ev_start, c->stream));
     MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_start, 0));
+    MMF_CUDA(cudaStreamWaitEvent(c->tr_stream, c->ev_start, 0));
     for (int b = 0; b < p.K; ++b) {
         long long base, count;
         band_cells(b, base, count);
@@ -778,12 +784,14 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     for (int b = 0; b < p.K; ++b) {
         long long base, count;
         band_cells(b, base, count);
-        MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_up[b], 0));
-        aos_to_soa_band_kernel<<<tr_blocks(count), 256, 0, c->stream>>>(c->aos, c->U, base, count, plane,
-                                                                         check_w ? c->flag : nullptr);
+        // the transpositions have a stream of the highest priority, so that the
+        // stage-1 kernels already running do not hold them back
+        MMF_CUDA(cudaStreamWaitEvent(c->tr_stream, c->ev_up[b], 0));
+        aos_to_soa_band_kernel<<<tr_blocks(count), 256, 0, c->tr_stream>>>(c->aos, c->U, base, count, plane,
+                                                                            check_w ? c->flag : nullptr);
         ++c->launches;
         MMF_CUDA(cudaPeekAtLastError());
-        MMF_CUDA(cudaEventRecord(c->ev_tr[b], c->stream));
+        MMF_CUDA(cudaEventRecord(c->ev_tr[b], c->tr_stream));
     }
     if (check_w) {
         MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr[p.K - 1], 0));

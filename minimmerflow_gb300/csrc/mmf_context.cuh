@@ -42,6 +42,7 @@ struct mmf_ctx {
     // per band and direction, pinned host words for the flag and the control block
     static constexpr int MAX_BANDS = 8;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t tr_stream = nullptr;            // upload transpositions, highest priority
     cudaStream_t band_stream[MAX_BANDS] = {};   // band b at priority b (band 0 first)
     cudaEvent_t ev_up[MAX_BANDS] = {}, ev_tr[MAX_BANDS] = {}, ev_s1[MAX_BANDS] = {}, ev_dn[MAX_BANDS] = {};
     cudaEvent_t ev_start = nullptr, ev_s2 = nullptr, ev_flag = nullptr;
