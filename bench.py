@@ -568,7 +568,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.n <= 0:
-        args.n = 1024 if args.workload == "sod2d" else 256
+        args.n = 1024 if args.workload in ("sod2d", "facelist") else 256
     world, rank, local, dist = dist_setup(args)
     workload = workload_config(args, world)
     metric = "cell-updates/s"
