@@ -675,6 +675,8 @@ def main():
                                 % (dom, r["case"].dim)),
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "peak_source": peak_src, "traffic": traffic,
+                     "limiting_unit": ("FP64 pipe: the HBM bound is the stated one, the kernels are bound by FP64 "
+                                       "issue (see the fp64 object and profiles/stage2d_fast_sod1024.md)"),
                      "algorithmic_bytes_per_launch": stage_bytes[dom] * ncell,
                      "stage_ms": {str(k): 1e3 * v for k, v in r["st_mean"].items()}},
         "fp64": {"ops_per_cell_update_model": fp64_ops,
