@@ -15,6 +15,7 @@
 #include "../../include/mmf_gb300.h"
 #include "mmf_batch.cuh"
 #include "mmf_launch.cuh"
+#include "mmf_nvtx.h"
 
 namespace mmf {
 int set_last_error(int code, const char *msg);
@@ -389,6 +390,7 @@ int mmf_batch_time_setup(mmf_batch *b, const double *cfl, const double *t_end, i
 
 int mmf_batch_advance_async(mmf_batch *b, int64_t n_steps)
 {
+    NvtxRange range_("mmf_batch_advance_async");
     int rc = batch_check(b);
     if (rc) return rc;
     if (!b->time_ready) return set_last_error(MMF_ERR_ARG, "mmf_batch_time_setup first");
@@ -460,6 +462,7 @@ int mmf_batch_set_indicator(mmf_batch *b, mmf_mlp *mlp, float threshold)
 
 int mmf_batch_autotune(mmf_batch *b, int trial_steps, int *chunk_out, int *blocks_per_sm_out)
 {
+    NvtxRange range_("mmf_batch_autotune");
     int rc = batch_check(b);
     if (rc) return rc;
     if (!b->time_ready) return set_last_error(MMF_ERR_ARG, "mmf_batch_time_setup first");

@@ -297,6 +297,7 @@ static int from_soa(mmf_ctx *c, const double *soa, double *d_aos, int64_t n_raw)
 
 int mmf_upload_state(mmf_ctx *c, const double *aos, int64_t n_raw)
 {
+    NvtxRange range_("mmf_upload_state");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
@@ -307,6 +308,7 @@ int mmf_upload_state(mmf_ctx *c, const double *aos, int64_t n_raw)
 
 int mmf_download_state(mmf_ctx *c, double *aos, int64_t n_raw)
 {
+    NvtxRange range_("mmf_download_state");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");
@@ -335,6 +337,7 @@ int mmf_download_state_device(mmf_ctx *c, double *d_aos, int64_t n_raw)
 
 int mmf_compute_rhs(mmf_ctx *c, const double *cons, double *rhs, double *max_eig, int64_t n_raw)
 {
+    NvtxRange range_("mmf_compute_rhs");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!cons || !rhs || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad buffers");
@@ -594,6 +597,7 @@ static int build_graph(mmf_ctx *c, int steps, cudaGraphExec_t *exec)
 
 int mmf_advance(mmf_ctx *c, int64_t n_steps, double *t_out, int64_t *steps_done)
 {
+    NvtxRange range_("mmf_advance");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
@@ -633,6 +637,7 @@ int mmf_advance(mmf_ctx *c, int64_t n_steps, double *t_out, int64_t *steps_done)
 
 int mmf_advance_async(mmf_ctx *c, int64_t n_steps)
 {
+    NvtxRange range_("mmf_advance_async");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
@@ -890,6 +895,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
 // and maxEig is a max), so only the speed changes.
 int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
 {
+    NvtxRange range_("mmf_autotune");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!c->time_ready) return fail(MMF_ERR_ARG, "mmf_time_setup first");
@@ -946,6 +952,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
 
 int mmf_advance_host(mmf_ctx *c, double *aos, int64_t n_raw, int64_t n_steps, double *t_out)
 {
+    NvtxRange range_("mmf_advance_host");
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!aos || n_raw != c->gp.plane) return fail(MMF_ERR_ARG, "bad state buffer");

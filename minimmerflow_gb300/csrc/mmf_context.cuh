@@ -6,6 +6,7 @@
 
 #include "../../include/mmf_gb300.h"
 #include "mmf_launch.cuh"
+#include "mmf_nvtx.h"
 
 namespace mmf {
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,

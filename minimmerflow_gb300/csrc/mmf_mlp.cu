@@ -12,6 +12,7 @@
 #include "../../include/mmf_gb300.h"
 #include "mmf_mlp.cuh"
 #include "mmf_mlp_train.cuh"
+#include "mmf_nvtx.h"
 
 namespace mmf {
 int set_last_error(int code, const char *msg);
@@ -223,6 +224,7 @@ int mmf_mlp_gradients(mmf_mlp *p, const void *d_X, const unsigned char *d_y, int
 
 int mmf_mlp_train_batch(mmf_mlp *p, const void *d_X, const unsigned char *d_y, int64_t B, float lr, float *loss_out)
 {
+    NvtxRange range_("mmf_mlp_train_batch");
     if (!p || !d_X || !d_y || !(lr > 0.0f)) return set_last_error(MMF_ERR_ARG, "bad argument");
     MLP_CUDA(cudaSetDevice(p->device));
     int rc = run_train(p, d_X, d_y, B);

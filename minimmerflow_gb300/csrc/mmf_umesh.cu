@@ -11,6 +11,7 @@
 
 #include "../../include/mmf_gb300.h"
 #include "mmf_umesh.cuh"
+#include "mmf_nvtx.h"
 
 namespace mmf {
 int set_last_error(int code, const char *msg);
@@ -281,6 +282,7 @@ int mmf_umesh_download(mmf_umesh *u, double *aos, int64_t n)
 
 int mmf_umesh_compute_rhs(mmf_umesh *u, const double *cons, double *rhs, double *max_eig, int64_t n)
 {
+    NvtxRange range_("mmf_umesh_compute_rhs");
     int rc = um_check(u);
     if (rc) return rc;
     if (!cons || !rhs || n != u->m.ncells) return set_last_error(MMF_ERR_ARG, "bad buffers");
@@ -322,6 +324,7 @@ int mmf_umesh_time_setup(mmf_umesh *u, double cfl, double t, double t_end, int64
 
 int mmf_umesh_advance(mmf_umesh *u, int64_t n_steps, double *t_out, int64_t *steps_done)
 {
+    NvtxRange range_("mmf_umesh_advance");
     int rc = um_check(u);
     if (rc) return rc;
     if (!u->time_ready) return set_last_error(MMF_ERR_ARG, "mmf_umesh_time_setup first");
