@@ -139,6 +139,14 @@ void *mmf_get_stream(mmf_ctx *ctx);
  * Needs mmf_time_setup.  warps_per_block is 0 in 3D.  No reference
  * counterpart. */
 int mmf_autotune(mmf_ctx *ctx, int trial_steps, int *chunk, int *warps_per_block);
+/* Per-step log, the values the reference prints each step (src/main.cpp:
+ * 399-404): maxEig, the dt used and the time after the step.  The device
+ * keeps the last 'capacity' steps in a ring (0 switches the log off).
+ * mmf_get_step_log copies up to max_entries of the most recent steps, oldest
+ * first, as out[3 * i + {0, 1, 2}] = {maxEig, dt, t}, with the index of the
+ * first one.  No reference counterpart (the reference writes a text log). */
+int mmf_set_step_log(mmf_ctx *ctx, int64_t capacity);
+int mmf_get_step_log(mmf_ctx *ctx, double *out, int64_t max_entries, int64_t *first_step, int64_t *n_entries);
 int mmf_advance_host(mmf_ctx *ctx, double *aos, int64_t n_raw, int64_t n_steps, double *t_out);
 /* Last step's dt and stage-1 maxEig (the reference logs both, main.cpp:399). */
 int mmf_last_step_info(mmf_ctx *ctx, double *dt, double *max_eig);

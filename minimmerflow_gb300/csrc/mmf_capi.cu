@@ -204,7 +204,7 @@ int mmf_destroy(mmf_ctx *c)
     if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
     cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
-    cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active);
+    cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active); cudaFree(c->steplog);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
@@ -571,6 +571,8 @@ int mmf_time_setup(mmf_ctx *c, double cfl, double t, double t_end, int64_t max_s
     h.t_end = t_end;
     h.cfl_h = 0.9 * cfl * c->grid.h;
     h.max_steps = (max_steps < 0) ? LLONG_MAX : max_steps;
+    h.log = c->steplog;
+    h.log_cap = c->steplog_cap;
     MMF_CUDA(cudaMemcpyAsync(c->ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     c->cfl = cfl;
@@ -888,6 +890,55 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     return MMF_OK;
 }
 
+// Per-step log (the reference's "Ideal dt ... (maxEig = ...)", "Using dt",
+// "Current time" lines, main.cpp:399-404): a device ring of 'capacity' steps
+// written by the stage-3 bookkeeping; capacity 0 switches it off.
+int mmf_set_step_log(mmf_ctx *c, int64_t capacity)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (capacity < 0) return fail(MMF_ERR_ARG, "capacity < 0");
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFree(c->steplog);
+    c->steplog = nullptr;
+    c->steplog_cap = 0;
+    if (capacity > 0) {
+        MMF_CUDA(cudaMalloc(&c->steplog, sizeof(double) * 3 * (size_t)capacity));
+        c->steplog_cap = capacity;
+    }
+    Ctrl h;
+    MMF_CUDA(cudaMemcpyAsync(&h, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    h.log = c->steplog;
+    h.log_cap = c->steplog_cap;
+    MMF_CUDA(cudaMemcpyAsync(c->ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    return MMF_OK;
+}
+
+int mmf_get_step_log(mmf_ctx *c, double *out, int64_t max_entries, int64_t *first_step, int64_t *n_entries)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!out || max_entries < 0 || !first_step || !n_entries) return fail(MMF_ERR_ARG, "bad arguments");
+    Ctrl h;
+    MMF_CUDA(cudaMemcpyAsync(&h, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    const long long avail = c->steplog ? std::min<long long>(h.step, c->steplog_cap) : 0;
+    const long long n = std::min<long long>(avail, max_entries);
+    std::vector<double> ring((size_t)(3 * c->steplog_cap));
+    if (n > 0)
+        MMF_CUDA(cudaMemcpy(ring.data(), c->steplog, sizeof(double) * ring.size(), cudaMemcpyDeviceToHost));
+    const long long first = h.step - n;
+    for (long long i = 0; i < n; ++i) {
+        const long long slot = (first + i) % c->steplog_cap;
+        for (int k = 0; k < 3; ++k) out[3 * i + k] = ring[(size_t)(3 * slot + k)];
+    }
+    *first_step = first;
+    *n_entries = n;
+    return MMF_OK;
+}
+
 // Chooses the decomposition (2D: rows per marching chunk and warps per block;
 // 3D: planes per chunk) by timing a few steps of each candidate from the
 // current state; the state and the time control are restored afterwards.
@@ -908,6 +959,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     Ctrl trial = saved;
     trial.t_end = HUGE_VAL;
     trial.max_steps = LLONG_MAX;
+    trial.log = nullptr;   // the trial steps are not steps of the run
     std::vector<std::pair<int, int>> cand;
     if (c->gp.dim == 2) {
         for (int ch : {8, 12, 16, 20, 24, 28, 30, 32, 40, 48, 64})

@@ -41,6 +41,8 @@ struct Ctrl {
     int active;                     // this step runs (t < t_end and step < max_steps)
     unsigned status;                // bit0 rho<0, bit1 p<0, bit2 NaN
     double last_maxeig;             // stage-1 maxEig of the last step (log)
+    double *log;                    // optional step log: per step (maxEig, dt, t after the step)
+    long long log_cap;              // entries of the log ring (step % log_cap)
 };
 
 struct GridParams {
@@ -130,6 +132,13 @@ __device__ __forceinline__ void step_bookkeeping(Ctrl *ctrl, const StepScalars &
     if (!sc.active) return;
     if (STAGE == STAGE_2) ctrl->dt = sc.dt;
     if (STAGE == STAGE_3) {
+        // main.cpp:399-404: the step's maxEig, dt and new time, as the reference logs them
+        if (ctrl->log) {
+            double *e = ctrl->log + 3 * (ctrl->step % ctrl->log_cap);
+            e[0] = __longlong_as_double((long long)ctrl->maxeig_bits);
+            e[1] = sc.dt;
+            e[2] = ctrl->t + sc.dt;
+        }
         // main.cpp:505-506; the stage-1 reduction slot is cleared for the next step
         ctrl->last_maxeig = __longlong_as_double((long long)ctrl->maxeig_bits);
         ctrl->t += sc.dt;

@@ -49,6 +49,9 @@ struct mmf_ctx {
     cudaEvent_t ev_start = nullptr, ev_s2 = nullptr, ev_flag = nullptr;
     int *h_flag = nullptr;
     Ctrl *h_ctrl = nullptr;
+    // optional per-step log (mmf_set_step_log): 3 doubles per step, a ring
+    double *steplog = nullptr;
+    long long steplog_cap = 0;
 
     cudaError_t stage(int st, const double *U_in, double *out) { return stage_gp(st, gp, U_in, out, stream); }
     // a stage over the rows (2D) / planes (3D) that 'g' covers, on stream 'on'

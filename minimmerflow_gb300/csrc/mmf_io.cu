@@ -148,7 +148,7 @@ GridGeom geom_of(const mmf_ctx *c)
     return g;
 }
 
-constexpr uint64_t CKPT_MAGIC = 0x3130504b43464d4dull;   // "MMFCKP01"
+constexpr uint64_t CKPT_MAGIC = 0x3230504b43464d4dull;   // "MMFCKP02"
 
 } // namespace
 
@@ -306,6 +306,8 @@ int mmf_load_checkpoint(mmf_ctx *c, const char *path)
               std::fread(&h, sizeof(Ctrl), 1, fp) == 1 && std::fread(u.data(), sizeof(double), u.size(), fp) == u.size();
     std::fclose(fp);
     if (!ok) return set_last_error(MMF_ERR_ARG, "checkpoint does not match this context");
+    h.log = c->steplog;          // the log of this context, not the one of the saved run
+    h.log_cap = c->steplog_cap;
     IO_CUDA(cudaMemcpyAsync(c->U, u.data(), sizeof(double) * NF * n, cudaMemcpyHostToDevice, c->stream));
     IO_CUDA(cudaMemcpyAsync(c->ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
     IO_CUDA(cudaStreamSynchronize(c->stream));

@@ -201,6 +201,17 @@ class CartesianEuler:
         capi.check(self._lib.mmf_autotune(self._ctx, trial_steps, C.byref(ch), C.byref(w)))
         return ch.value, w.value
 
+    def set_step_log(self, capacity):
+        """Keep (maxEig, dt, t) of the last 'capacity' steps on the device."""
+        capi.check(self._lib.mmf_set_step_log(self._ctx, capacity))
+
+    def step_log(self, max_entries=1 << 20):
+        """(first step index, array [n, 3] of maxEig, dt, t after the step)."""
+        out = np.empty((max_entries, 3))
+        first, n = C.c_int64(), C.c_int64()
+        capi.check(self._lib.mmf_get_step_log(self._ctx, capi.ptr(out), max_entries, C.byref(first), C.byref(n)))
+        return first.value, out[:n.value].copy()
+
     def init_state(self, case):
         """Initial state of a problem case computed on the device (problem.cpp:247-392)."""
         capi.check(self._lib.mmf_init_state(self._ctx, C.byref(problem_struct(case))))

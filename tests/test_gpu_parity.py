@@ -342,3 +342,28 @@ def test_advance_stops_at_the_end_time(mmf):
         t, steps = s.advance(1 << 24)
         assert time.perf_counter() - t0 < 5.0
         assert t == 0.05 and steps > 0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_step_log_matches_the_reference_loop(orc, mmf, order):
+    """The device step log holds, per step, the values the reference logs
+    (main.cpp:399-404): the first stage's maxEig, the dt used (0.9 CFL h /
+    maxEig, clamped to the end time) and the time after the step -- bit for
+    bit with the reference arithmetic against the oracle's own log of the
+    same run.  A ring of 8 keeps the last 8 of 12 steps."""
+    case = mmf.problem.reference_case("radsod", 2, 32, t_end=1.0)
+    m = oracle_mesh(orc, case)
+    U0 = case.initial_state()
+    _, _, steps, dtl, mel = m.run(U0, case.cfl, t_end=1.0, max_steps=12, order=order, log=True)
+    assert steps == 12
+    t_ref = np.cumsum(np.concatenate([[0.0], dtl[:12]]))   # sequential sums, as t += dt
+    with case.solver(arith="reference", order=order) as s:
+        s.set_step_log(8)
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, 1.0)
+        s.advance(12)
+        first, log = s.step_log()
+    assert first == 4 and log.shape == (8, 3)
+    np.testing.assert_array_equal(log[:, 0], mel[4:12])
+    np.testing.assert_array_equal(log[:, 1], dtl[4:12])
+    np.testing.assert_array_equal(log[:, 2], t_ref[5:13])
