@@ -140,6 +140,14 @@ def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    try:
+        import torch
+        ndev = torch.cuda.device_count()
+    except Exception:
+        ndev = 0
+    if ndev > 0:
+        # more replicas than visible GPUs share them round-robin
+        local %= ndev
     dist = None
     if world > 1:
         import torch.distributed as dist
