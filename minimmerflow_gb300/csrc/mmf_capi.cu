@@ -215,7 +215,7 @@ int mmf_destroy(mmf_ctx *c)
     }
     for (int b = 0; b < mmf_ctx::MAX_BANDS; ++b) {
         if (c->band_stream[b]) { cudaStreamSynchronize(c->band_stream[b]); cudaStreamDestroy(c->band_stream[b]); }
-        cudaEvent_t evs[4] = {c->ev_up[b], c->ev_tr[b], c->ev_s1[b], c->ev_dn[b]};
+        cudaEvent_t evs[5] = {c->ev_up[b], c->ev_tr[b], c->ev_s1[b], c->ev_dn[b], c->ev_s2b[b]};
         for (cudaEvent_t e : evs) if (e) cudaEventDestroy(e);
     }
     if (c->ev_start) cudaEventDestroy(c->ev_start);
@@ -676,17 +676,24 @@ void *mmf_get_stream(mmf_ctx *c) { return c ? (void *)c->stream : nullptr; }
 // ---- pipelined host round trip ------------------------------------------
 // The state is cut into K bands along the slowest axis (rows in 2D, planes in
 // 3D).  Band b's upload (copy stream) overlaps the transposition and the
-// stage-1 kernels of the bands already on the device; after stage 2, each
-// band's stage 3 is followed by its transposition and its download (copy
-// stream), which overlaps the stage 3 of the next band.  Stage 2 needs the
-// step's dt, a max over every cell of stage 1, so it runs on the whole grid.
-// The stage-1 band kernels run on one stream per band (band 0 at the highest
-// priority) so that they overlap one another and the transpositions; the
-// stage-3 bands are issued in band order on two streams taken in turn, so that
-// a band's launch overlaps the end of the previous one while the first
-// downloads still start early.  Band launches march short chunks so that
-// each has work for every SM.
+// stage-1 kernels of the bands already on the device; the stage-1 band
+// kernels run on one stream per band (band 0 at the highest priority) so that
+// they overlap one another and the transpositions.  Stage 2 needs the step's
+// dt, a max over every cell of stage 1, so it starts once stage 1 is done
+// everywhere; in the last step it then runs band by band, each band's stage 3
+// follows as soon as stage 2 is done on the rows it reads, and each band's
+// stage 3 is followed by its transposition and its download (copy stream):
+// bands finish in order and the downloads overlap the rest of the step.
+// Band launches march short chunks so that each has work for every SM.
 static constexpr int S3_STREAMS = 2;   // streams the stage-3 bands take in turn
+static constexpr int S2_STREAMS = 2;   // streams the stage-2 bands take in turn
+
+// The i-th stage-3 band launch takes the band streams of the highest
+// priorities in turn; the i-th stage-2 band launch the next ones.  At most
+// S2_STREAMS + S3_STREAMS band kernels then share the GPU, enough to fill it,
+// so that bands finish roughly in order and the downloads start early.
+static cudaStream_t s3_stream(mmf_ctx *c, int i) { return c->band_stream[i % S3_STREAMS]; }
+static cudaStream_t s2_stream(mmf_ctx *c, int i) { return c->band_stream[S3_STREAMS + i % S2_STREAMS]; }
 
 struct BandPlan {
     int K = 0;
@@ -726,6 +733,7 @@ static GridParams band_params(const mmf_ctx *c, const BandPlan &p, int b, int bo
     return g;
 }
 
+
 static int pipeline_resources(mmf_ctx *c)
 {
     if (c->copy_stream) return MMF_OK;
@@ -740,6 +748,7 @@ static int pipeline_resources(mmf_ctx *c)
         MMF_CUDA(cudaEventCreateWithFlags(&c->ev_tr[b], cudaEventDisableTiming));
         MMF_CUDA(cudaEventCreateWithFlags(&c->ev_s1[b], cudaEventDisableTiming));
         MMF_CUDA(cudaEventCreateWithFlags(&c->ev_dn[b], cudaEventDisableTiming));
+        MMF_CUDA(cudaEventCreateWithFlags(&c->ev_s2b[b], cudaEventDisableTiming));
     }
     MMF_CUDA(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
     MMF_CUDA(cudaEventCreateWithFlags(&c->ev_s2, cudaEventDisableTiming));
@@ -768,6 +777,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     const long long plane = gp.plane;
     const bool periodic_slow = (gp.dim == 2 ? gp.bc_lo[1] : gp.bc_lo[2]) == BC_PERIODIC;
     const bool check_w = gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST;
+    const int K = p.K;
     auto band_cells = [&](int b, long long &base, long long &count) {
         const int r0 = b * p.rows, r1 = std::min(p.n_slow, r0 + p.rows);
         base = (long long)r0 * p.slab;
@@ -781,14 +791,14 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     MMF_CUDA(cudaEventRecord(c->ev_start, c->stream));
     MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_start, 0));
     MMF_CUDA(cudaStreamWaitEvent(c->tr_stream, c->ev_start, 0));
-    for (int b = 0; b < p.K; ++b) {
+    for (int b = 0; b < K; ++b) {
         long long base, count;
         band_cells(b, base, count);
         MMF_CUDA(cudaMemcpyAsync(c->aos + NF * base, aos + NF * base, sizeof(double) * NF * count,
                                  cudaMemcpyHostToDevice, c->copy_stream));
         MMF_CUDA(cudaEventRecord(c->ev_up[b], c->copy_stream));
     }
-    for (int b = 0; b < p.K; ++b) {
+    for (int b = 0; b < K; ++b) {
         long long base, count;
         band_cells(b, base, count);
         // the transpositions have a stream of the highest priority, so that the
@@ -801,7 +811,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
         MMF_CUDA(cudaEventRecord(c->ev_tr[b], c->tr_stream));
     }
     if (check_w) {
-        MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr[p.K - 1], 0));
+        MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tr[K - 1], 0));
         MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
         MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
     }
@@ -812,10 +822,10 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     {
         const int nch = (p.n_slow + p.chunk - 1) / p.chunk;
         int next = periodic_slow ? 1 : 0;   // first chunk not yet launched
-        for (int b = 0; b < p.K; ++b) {
+        for (int b = 0; b < K; ++b) {
             const int rb = std::min(p.n_slow, (b + 1) * p.rows);
-            int upto = (b == p.K - 1) ? nch : (rb - 1) / p.chunk;   // chunks [next, upto) are ready
-            const bool first0 = periodic_slow && b == p.K - 1;
+            int upto = (b == K - 1) ? nch : (rb - 1) / p.chunk;   // chunks [next, upto) are ready
+            const bool first0 = periodic_slow && b == K - 1;
             MMF_CUDA(cudaStreamWaitEvent(c->band_stream[b], c->ev_tr[b], 0));
             if (upto > next || first0) {
                 GridParams g = c->gp;
@@ -836,7 +846,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             MMF_CUDA(cudaEventRecord(c->ev_s1[b], c->band_stream[b]));
         }
     }
-    for (int q = 0; q < p.K; ++q) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_s1[q], 0));
+    for (int q = 0; q < K; ++q) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_s1[q], 0));
     if (check_w) {
         // the stage-1 kernels used the previous z-momentum choice; redo stage 1
         // on the whole grid if this state does not fit it
@@ -856,22 +866,54 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     }
     for (int64_t s = 0; s < n_steps; ++s) {
         if (s > 0) MMF_CUDA(c->stage(STAGE_1, c->U, c->R));
-        MMF_CUDA(c->stage(STAGE_2, c->U, c->W));
         if (s + 1 < n_steps) {
+            MMF_CUDA(c->stage(STAGE_2, c->U, c->W));
             MMF_CUDA(c->stage(STAGE_3, c->U, c->U));
             continue;
         }
-        // last step: stage 3, transposition and download, band by band, in
-        // band order on S3_STREAMS streams taken in turn (so that a band's
-        // launch overlaps the end of the previous one while the early bands
-        // still finish first and their downloads start early)
-        MMF_CUDA(cudaEventRecord(c->ev_s2, c->stream));
-        for (int b = 0; b < p.K; ++b) {
+        // last step: stage 2 band by band once stage 1 is done everywhere (dt),
+        // stage 3 of a band once stage 2 is done on its rows and the two
+        // neighbour rows, then its transposition and its download
+        MMF_CUDA(cudaEventRecord(c->ev_s2, c->stream));   // stage 1 done
+        for (int b = 0; b < K; ++b) {
+            cudaStream_t bs = s2_stream(c, b);
+            if (b < S2_STREAMS) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2, 0));
+            // band 0 writes dt to the control block for stage 3
+            MMF_CUDA(c->stage_gp(STAGE_2, band_params(c, p, b, b == 0), c->U, c->W, bs));
+            MMF_CUDA(cudaEventRecord(c->ev_s2b[b], bs));
+        }
+        // stage-2 bands a stage-3 band waits for: its own, those of its two
+        // neighbour rows (wrapped on a periodic slow axis; stage 3 writes U in
+        // place, which those stage-2 bands read) and band 0 (dt).  Bands are
+        // issued in the order their stage-2 inputs complete.
+        std::vector<unsigned> dep(K);
+        std::vector<int> order(K);
+        for (int b = 0; b < K; ++b) {
+            unsigned m = 1u | (1u << b);
+            if (b > 0) m |= 1u << (b - 1);
+            else if (periodic_slow) m |= 1u << (K - 1);
+            if (b + 1 < K) m |= 1u << (b + 1);
+            else if (periodic_slow) m |= 1u;
+            dep[b] = m;
+            order[b] = b;
+        }
+        auto ready = [&](int b) {   // the last stage-2 band it needs
+            int r = 0;
+            for (int q = 0; q < K; ++q) if (dep[b] & (1u << q)) r = q;
+            return r;
+        };
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ready(x) < ready(y); });
+        for (int i = 0; i < K; ++i) {
+            const int b = order[i];
+            cudaStream_t bs = s3_stream(c, i);
+            // the last stage-3 launch advances the step in the control block
+            // once every stage-2 band has read it
+            const bool last = (i == K - 1);
+            for (int q = 0; q < K; ++q)
+                if (last || (dep[b] & (1u << q))) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2b[q], 0));
+            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, last), c->U, c->U, bs));
             long long base, count;
             band_cells(b, base, count);
-            cudaStream_t bs = c->band_stream[b % S3_STREAMS];
-            if (b < S3_STREAMS) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2, 0));
-            MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, b == p.K - 1), c->U, c->U, bs));
             soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, bs>>>(c->U, c->aos, base, count, plane);
             ++c->launches;
             MMF_CUDA(cudaPeekAtLastError());
@@ -880,8 +922,8 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             MMF_CUDA(cudaMemcpyAsync(aos + NF * base, c->aos + NF * base, sizeof(double) * NF * count,
                                      cudaMemcpyDeviceToHost, c->copy_stream));
         }
-        for (int b = 0; b < p.K; ++b) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_dn[b], 0));
     }
+    for (int b = 0; b < K; ++b) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_dn[b], 0));
     MMF_CUDA(cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream));
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     MMF_CUDA(cudaStreamSynchronize(c->copy_stream));
