@@ -77,8 +77,8 @@ __device__ __forceinline__ double mc_slope_bits(double a, double b, double centr
     const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
     if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;
-    const double m = __longlong_as_double(ma < mb ? ma : mb);
-    const long long m2 = __double_as_longlong(m + m), mc = abs_bits(central);
+    const long long m2 = __double_as_longlong(twice_exact(__longlong_as_double(ma < mb ? ma : mb)));
+    const long long mc = abs_bits(central);
     return __longlong_as_double((m2 < mc ? m2 : mc) | (ia & (long long)0x8000000000000000ull));
 }
 
@@ -99,7 +99,7 @@ __device__ __forceinline__ bool admissible(const double *c)
     if (!(ir > 0 && ir <= inf)) return false;
     double m2 = fma(c[2], c[2], c[1] * c[1]);
     if (NV == 5) m2 = fma(c[3], c[3], m2);
-    const long long iq = __double_as_longlong(fma(2.0 * c[0], c[NV - 1], -m2));
+    const long long iq = __double_as_longlong(fma(twice_exact(c[0]), c[NV - 1], -m2));
     return iq > 0 && iq <= inf;
 }
 
@@ -160,7 +160,7 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
         for (int k = 0; k < NV; ++k) {
             const double a = uc[k] - ul[k];
             const double b = ur[k] - uc[k];
-            const double central = 0.5 * (a + b);
+            const double central = IsExact<A>::value ? 0.5 * (a + b) : half_ftz(a + b);
             double sl = central;
             if (limit) {
                 // the activity is only recorded where a caller keeps it (stage 1)

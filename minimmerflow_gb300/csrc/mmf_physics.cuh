@@ -141,6 +141,30 @@ __device__ __forceinline__ double rcp_newton(double x)
     return fma(y, fma(e, e, e), y);
 }
 
+// x / 2 and 2 x by moving the exponent field (integer pipe; the FP64 pipe
+// is the narrow one).  Exact wherever the result is a normal number; half_ftz
+// flushes results below the normal range to a signed zero, twice_exact doubles
+// zero and subnormal x by a shift of the significand; infinities and NaNs keep
+// their value (and twice_exact does not guard against overflow: it is used
+// on physical magnitudes, far below 1e308).
+__device__ __forceinline__ double half_ftz(double x)
+{
+    const long long ix = __double_as_longlong(x);
+    const long long e = ix & 0x7ff0000000000000ll;
+    if (e == 0x7ff0000000000000ll) return x;
+    return __longlong_as_double(e > 0x0010000000000000ll ? ix - 0x0010000000000000ll
+                                                         : ix & (long long)0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double twice_exact(double x)
+{
+    const long long ix = __double_as_longlong(x);
+    const long long e = ix & 0x7ff0000000000000ll;
+    if (e == 0x7ff0000000000000ll) return x;
+    const long long sign = ix & (long long)0x8000000000000000ull;
+    return __longlong_as_double(e != 0 ? ix + 0x0010000000000000ll : ((ix ^ sign) << 1) | sign);
+}
+
 // Square root by the coupled Newton iteration on s ~ sqrt(x) and
 // r ~ 1/(2 sqrt(x)) (Goldschmidt's form), seeded with rsqrt.approx.ftz.f64,
 // followed by one Newton correction s <- s + r (x - s^2).  x >= 0; x = 0
@@ -150,7 +174,7 @@ __device__ __forceinline__ double sqrt_newton(double x)
     double y;
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
     double s = x * y;
-    double r = 0.5 * y;
+    double r = half_ftz(y);
     const double e = fma(-s, r, 0.5);
     s = fma(s, e, s);
     r = fma(r, e, r);

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) uface_kernel(UMesh m, const double *state
 #pragma unroll
                 for (int k = 0; k < NF; ++k) F[k] = ar * F[k];
             } else {
-                lam = fast_split(co, ro, cn, rn, nrm, 0.5 * ar, F);
+                lam = fast_split(co, ro, cn, rn, nrm, half_ftz(ar), F);
             }
             lmax = max_nonneg(lmax, lam);
         }
@@ -219,9 +219,11 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
             double u[NF];
             uload(state, n, c, u);
             const double m2 = fma(u[3], u[3], fma(u[2], u[2], u[1] * u[1]));
-            const double q = fma(2.0 * u[0], u[4], -m2);
-            status |= state_flags(u[0], u[0] > 0.0 ? q : 0.0);
-            if (q != q) status |= 4u;
+            const double q = fma(twice_exact(u[0]), u[4], -m2);
+            // compares on the bit patterns (integer pipe): rho > 0, q NaN
+            const long long ir = __double_as_longlong(u[0]), iq = __double_as_longlong(q);
+            status |= state_flags(u[0], (ir > 0 && ir <= 0x7ff0000000000000ll) ? q : 0.0);
+            if ((iq & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) status |= 4u;
         }
         if (solved) {
             const long long e = m.csr_off[c + 1];
