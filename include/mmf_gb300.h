@@ -338,6 +338,15 @@ int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_cons, double *
  * for positive x.  No reference counterpart; used to check the error bound. */
 int mmf_newton_selftest(int64_t n, const double *x, double *rcp, double *sqrt_out);
 
+/* Self-test of the FP32 screen of the order-2 positivity fallback: for each of
+ * n cells (uc [n][nv] stored fields, sig [n][dim][nv] slopes), dec[i] = 1 (every
+ * face state U -+ sigma/2 has rho > 0 and p > 0), 0 (some has not) or -1
+ * (undecided in FP32), and ref[i] = the FP64 test of the same arithmetic.
+ * nv = 4 is the 2D four-field layout (rho, rho u, rho v, rho E) of
+ * MMF_ARITH_FAST.  No reference counterpart; a decided dec must equal ref. */
+int mmf_o2_screen_selftest(int arith, int nv, int dim, int64_t n, const double *uc, const double *sig, int *dec,
+                           unsigned char *ref);
+
 #ifdef __cplusplus
 }
 #endif

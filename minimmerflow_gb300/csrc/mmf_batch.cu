@@ -165,6 +165,7 @@ static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
         for (int k = 0; k < NF; ++k) gp.dir_prim[k] = g.dirichlet_prim[k];
         gp.area = g.h;
         gp.vol = g.h * g.h;
+        gp.half_area_per_vol = 0.5 * gp.area / gp.vol;
         plan_cartesian(gp, chunk);
         gp.plane = b->total;
         hc[(size_t)c].offset = b->offsets[(size_t)c];

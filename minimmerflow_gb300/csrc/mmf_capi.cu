@@ -166,6 +166,7 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     const double h = grid->h;
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;
+    gp.half_area_per_vol = 0.5 * gp.area / gp.vol;
     plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D);
     const size_t bytes = sizeof(double) * NF * (size_t)gp.plane;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -1219,6 +1220,36 @@ int mmf_newton_selftest(int64_t n, const double *x, double *rcp, double *sqrt_ou
     if (e == cudaSuccess) e = cudaMemcpy(rcp, dr, b, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(sqrt_out, dq, b, cudaMemcpyDeviceToHost);
     cudaFree(dx); cudaFree(dr); cudaFree(dq);
+    if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
+    return MMF_OK;
+}
+
+int mmf_o2_screen_selftest(int arith, int nv, int dim, int64_t n, const double *uc, const double *sig, int *dec,
+                           unsigned char *ref)
+{
+    if (!uc || !sig || !dec || !ref || n < 0) return fail(MMF_ERR_ARG, "bad buffers");
+    if ((dim != 2 && dim != 3) || (nv != 4 && nv != 5) || (nv == 4 && (dim != 2 || arith != MMF_ARITH_FAST)) ||
+        (arith != MMF_ARITH_FAST && arith != MMF_ARITH_REFERENCE))
+        return fail(MMF_ERR_ARG, "unsupported arithmetic / field count / dimension");
+    if (n == 0) return MMF_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(MMF_ERR_CUDA, "no CUDA device available");
+    const size_t bu = sizeof(double) * (size_t)n * nv, bs = bu * dim;
+    double *du = nullptr, *ds = nullptr;
+    int *dd = nullptr;
+    unsigned char *dr = nullptr;
+    cudaError_t e = cudaMalloc(&du, bu);
+    if (e == cudaSuccess) e = cudaMalloc(&ds, bs);
+    if (e == cudaSuccess) e = cudaMalloc(&dd, sizeof(int) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&dr, (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(du, uc, bu, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ds, sig, bs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = arith == MMF_ARITH_FAST ? launch_screen_selftest_fast(nv, dim, n, du, ds, dd, dr, 0)
+                                    : launch_screen_selftest_exact(dim, n, du, ds, dd, dr, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(dec, dd, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ref, dr, (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(du); cudaFree(ds); cudaFree(dd); cudaFree(dr);
     if (e != cudaSuccess) return fail(MMF_ERR_CUDA, cudaGetErrorString(e));
     return MMF_OK;
 }

@@ -51,6 +51,7 @@ struct GridParams {
     int bc_lo[3], bc_hi[3];
     double dir_prim[NF];
     double area, vol;
+    double half_area_per_vol;   // 0.5 area / vol: the fast arithmetic's stage scale per unit dt
     int chunk;      // rows (2D) / planes (3D) per marching chunk
     int nseg;       // x segments of 30 cells
     int nrowblk;    // 3D: row blocks in y
@@ -71,6 +72,25 @@ struct StageArgs {
 };
 
 constexpr int SEG = 30;   // output cells per warp row
+
+// Grid coordinates of cell g (x fastest).  Grids of fewer than 2^32 cells
+// take 32-bit unsigned division: a 64-bit integer division by a run-time
+// divisor is a sequence of FP64 reciprocal steps, dear on this GPU.
+__device__ __forceinline__ void cell_coords(const GridParams &gp, long long g, int &x, int &y, int &z)
+{
+    if (gp.plane <= 0xffffffffll) {
+        const unsigned u = (unsigned)g, nx = (unsigned)gp.n[0], ny = (unsigned)gp.n[1];
+        const unsigned q = u / nx;
+        x = (int)(u - q * nx);
+        y = (int)(q % ny);
+        z = (int)(q / ny);
+    } else {
+        const long long q = g / gp.n[0];
+        x = (int)(g - q * gp.n[0]);
+        y = (int)(q % gp.n[1]);
+        z = (int)(q / gp.n[1]);
+    }
+}
 
 enum { STAGE_RHS = 0, STAGE_1 = 1, STAGE_2 = 2, STAGE_3 = 3 };
 
@@ -118,7 +138,7 @@ __device__ __forceinline__ StepScalars step_scalars(const GridParams &gp, const 
     } else {
         sc.dt = ctrl->dt;
     }
-    sc.s = IsExact<A>::value ? sc.dt : 0.5 * gp.area * sc.dt / gp.vol;
+    sc.s = IsExact<A>::value ? sc.dt : sc.dt * gp.half_area_per_vol;
     return sc;
 }
 

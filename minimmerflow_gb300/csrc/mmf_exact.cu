@@ -12,6 +12,12 @@ cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs 
     return launch_stage<ExactArith>(stage, gp, sa, s);
 }
 
+cudaError_t launch_screen_selftest_exact(int dim, long long n, const double *uc, const double *sig, int *dec,
+                                        unsigned char *ref, cudaStream_t s)
+{
+    return launch_screen_selftest<ExactArith>(dim, n, uc, sig, dec, ref, s);
+}
+
 cudaError_t launch_o2_exact(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
                             double *W1, cudaStream_t s)
 {

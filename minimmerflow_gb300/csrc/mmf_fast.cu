@@ -52,6 +52,13 @@ __global__ void newton_selftest_kernel(long long n, const double *x, double *r, 
     q[i] = sqrt_newton(x[i]);
 }
 
+cudaError_t launch_screen_selftest_fast(int nv, int dim, long long n, const double *uc, const double *sig, int *dec,
+                                       unsigned char *ref, cudaStream_t s)
+{
+    if (nv == 4) return launch_screen_selftest<FastArith2DW0>(dim, n, uc, sig, dec, ref, s);
+    return launch_screen_selftest<FastArith>(dim, n, uc, sig, dec, ref, s);
+}
+
 cudaError_t launch_newton_selftest(long long n, const double *x, double *r, double *q, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;

@@ -128,6 +128,13 @@ cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageA
 cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
 cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s, bool w_zero);
 
+// Self-test of the FP32 positivity screen of the order-2 slopes (nv 4: the 2D
+// four-field layout of the fast arithmetic).
+cudaError_t launch_screen_selftest_fast(int nv, int dim, long long n, const double *uc, const double *sig, int *dec,
+                                       unsigned char *ref, cudaStream_t s);
+cudaError_t launch_screen_selftest_exact(int dim, long long n, const double *uc, const double *sig, int *dec,
+                                        unsigned char *ref, cudaStream_t s);
+
 // Reciprocal and square root of the fast arithmetic, for the self-test.
 cudaError_t launch_newton_selftest(long long n, const double *x, double *r, double *q, cudaStream_t s);
 

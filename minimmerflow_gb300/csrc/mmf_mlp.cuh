@@ -116,7 +116,9 @@ __device__ __forceinline__ void cell_features(const double *U, const GridParams 
 {
     constexpr int NS = DIM == 3 ? 27 : 9;
     const int nx = gp.n[0], ny = gp.n[1];
-    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = DIM == 3 ? (int)(g / ((long long)nx * ny)) : 0;
+    int x, y, z;
+    cell_coords(gp, g, x, y, z);
+    if (DIM == 2) z = 0;
     float q[NS][5];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {

@@ -121,6 +121,7 @@ extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_con
     const double h = grid->h;
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;
+    gp.half_area_per_vol = 0.5 * gp.area / gp.vol;
     plan_cartesian(gp, grid->chunk);
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);

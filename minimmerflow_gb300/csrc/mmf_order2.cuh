@@ -117,6 +117,127 @@ __device__ __forceinline__ void load_plain(const double *planes, long long plane
     for (int k = 0; k < A::NVAR; ++k) c[k] = __ldg(planes + (long long)A::field(k) * plane + g);
 }
 
+// Positivity of the face states U -+ sigma_d / 2 of a cell, in FP64 (the
+// arithmetic's own operations).
+template <class A, int DIM>
+__device__ __forceinline__ bool faces_admissible(const double *uc, const double (*sig)[A::NVAR])
+{
+    constexpr int NV = A::NVAR;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        double fm[NV], fp[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            fm[k] = IsExact<A>::value ? uc[k] - 0.5 * sig[d][k] : fma(-0.5, sig[d][k], uc[k]);
+            fp[k] = face_value<A>(uc[k], 0.5, sig[d][k]);
+        }
+        ok = ok && admissible<A>(fm) && admissible<A>(fp);
+    }
+    return ok;
+}
+
+// x / 2^(emax - 1023) as a float (the value with exponent field emax maps to
+// [1, 2)), its significand truncated to 20 bits, on the integer pipe; scaled
+// magnitudes below 2^-126 flush to 0.  Error < 2^-20 |result| + 2^-126.
+__device__ __forceinline__ float scaled_f32(double x, int emax)
+{
+    const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32);
+    const int e = (int)((hi >> 20) & 0x7ff) - emax + 127;
+    return e > 0 ? __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3)) : 0.0f;
+}
+
+// The positivity test of faces_admissible decided in FP32 where the margins
+// allow it: 1 = every face state has rho > 0 and 2 rho E > |m|^2, 0 = some
+// face state has not, -1 = undecided.  FP64 instructions cost about as much
+// as 30 FP32 ones on this GPU, so the FP32 screen with an FP64 fallback for
+// the undecided cells is the cheaper route to the same answer.
+//
+// The cell's values are scaled by a common power of two and truncated
+// (scaled_f32).  Each FP32 face value carries a bound e_k at least 3.7 times
+// its distance to the FP64 face value (truncation 2^-20, FP32 rounding 2^-24,
+// FP64 rounding 2^-53, relative to |u| + |sigma|/2; flushing, absolute), and
+// the bound of Q = 2 rho E - |m|^2 doubles the propagated error and adds 2^-20
+// of the magnitudes for the roundings of Q itself (FP32, and FP64 in the
+// test it replaces) and 2^-100 for underflowed terms.  A sign decided
+// outside these bounds is the sign of the FP64 evaluation.
+template <class A, int DIM>
+__device__ __forceinline__ int screen_faces(const double *uc, const double (*sig)[A::NVAR])
+{
+    constexpr int NV = A::NVAR;
+    constexpr int IE = NV - 1;
+    int emax = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) emax = max(emax, (int)((__double_as_longlong(uc[k]) >> 52) & 0x7ff));
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) emax = max(emax, (int)((__double_as_longlong(sig[d][k]) >> 52) & 0x7ff));
+    if (emax >= 0x7ff) return -1;   // an infinity or a NaN
+    float u[NV], au[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { u[k] = scaled_f32(uc[k], emax); au[k] = fabsf(u[k]); }
+    bool sure_ok = true, sure_bad = false;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        float sg[NV], e[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sg[k] = scaled_f32(sig[d][k], emax);
+            e[k] = fmaf(0x1p-18f, fmaf(0.5f, fabsf(sg[k]), au[k]), 0x1p-120f);
+        }
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            float f[NV], af[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { f[k] = fmaf(side ? 0.5f : -0.5f, sg[k], u[k]); af[k] = fabsf(f[k]); }
+            float m2 = 0.0f, em = 0.0f;
+#pragma unroll
+            for (int k = 1; k < IE; ++k) {
+                m2 = fmaf(f[k], f[k], m2);
+                em = fmaf(e[k], fmaf(2.0f, af[k], e[k]), em);
+            }
+            const float Q = fmaf(2.0f * f[0], f[IE], -m2);
+            const float eQ = fmaf(2.0f, fmaf(2.0f, fmaf(e[0], af[IE], fmaf(e[IE], af[0], e[0] * e[IE])), em),
+                                  fmaf(0x1p-20f, fmaf(2.0f * af[0], af[IE], m2), 0x1p-100f));
+            sure_ok = sure_ok && (f[0] > e[0]) && (Q > eQ);
+            sure_bad = sure_bad || (f[0] < -e[0]) || (Q < -eQ);
+        }
+    }
+    return sure_bad ? 0 : (sure_ok ? 1 : -1);
+}
+
+// Self-test of screen_faces: for each sample, the FP32 decision and the FP64
+// test it stands for (uc [n][NV], sig [n][DIM][NV]).
+template <class A, int DIM>
+__global__ void __launch_bounds__(128) screen_selftest_kernel(long long n, const double *uc, const double *sig,
+                                                              int *dec, unsigned char *ref)
+{
+    constexpr int NV = A::NVAR;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double u[NV], s[DIM][NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) u[k] = uc[i * NV + k];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) s[d][k] = sig[(i * DIM + d) * NV + k];
+    dec[i] = screen_faces<A, DIM>(u, s);
+    ref[i] = faces_admissible<A, DIM>(u, s) ? 1 : 0;
+}
+
+template <class A>
+inline cudaError_t launch_screen_selftest(int dim, long long n, const double *uc, const double *sig, int *dec,
+                                          unsigned char *ref, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    if (dim == 2) screen_selftest_kernel<A, 2><<<blocks, 128, 0, st>>>(n, uc, sig, dec, ref);
+    else screen_selftest_kernel<A, 3><<<blocks, 128, 0, st>>>(n, uc, sig, dec, ref);
+    return cudaPeekAtLastError();
+}
+
 // computePolynomials of grid cell g (index inside the grid; field planes of
 // the grid are gp.plane apart).
 template <class A, int DIM>
@@ -125,10 +246,8 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
     constexpr int NV = A::NVAR;
     const int nx = gp.n[0], ny = gp.n[1];
     const long long n = gp.plane;
-    const int ix = (int)(g % nx);
-    const int iy = (int)((g / nx) % ny);
-    const int iz = (DIM == 3) ? (int)(g / ((long long)nx * ny)) : 0;
-    const int idx[3] = {ix, iy, iz};
+    int idx[3];
+    cell_coords(gp, g, idx[0], idx[1], idx[2]);
     double uc[NV];
     load_plain<A>(oa.state, n, g, uc);
     const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
@@ -176,18 +295,11 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
         }
     }
     if (limit || oa.limit_mode == LIMIT_FLAGGED) {
-        // positivity fallback, also for the cells a flag leaves on central slopes
-        bool ok = true;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            double fm[NV], fp[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                fm[k] = IsExact<A>::value ? uc[k] - 0.5 * sig[d][k] : fma(-0.5, sig[d][k], uc[k]);
-                fp[k] = face_value<A>(uc[k], 0.5, sig[d][k]);
-            }
-            ok = ok && admissible<A>(fm) && admissible<A>(fp);
-        }
+        // positivity fallback, also for the cells a flag leaves on central
+        // slopes; decided in FP32 where the margins allow, else in FP64
+        const int dec = screen_faces<A, DIM>(uc, sig);
+        bool ok = dec > 0;
+        if (dec < 0) ok = faces_admissible<A, DIM>(uc, sig);
         if (!ok) {
 #pragma unroll
             for (int d = 0; d < DIM; ++d)
@@ -236,10 +348,11 @@ __global__ void __launch_bounds__(256) form_w1_kernel(GridParams gp, StageArgs s
     if (blockIdx.x == 0 && threadIdx.x == 0 && sc.active) sa.ctrl->dt = sc.dt;
     if (!sc.active) return;
     const long long n = gp.plane;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)A::NVAR * n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long o = (long long)A::field((int)(i / n)) * n + i % n;
-        W1[o] = form_w1_value<A>(sa, gp, sc, o);
+#pragma unroll
+    for (int k = 0; k < A::NVAR; ++k) {
+        const long long base = (long long)A::field(k) * n;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            W1[base + i] = form_w1_value<A>(sa, gp, sc, base + i);
     }
 }
 

@@ -61,6 +61,7 @@ struct mmf_umesh {
     double min_size = 0.0;
     // device arrays
     double *vol = nullptr, *area = nullptr, *normal = nullptr;
+    double *inv_vol = nullptr;   // fast arithmetic: 1 / volume per cell
     unsigned char *solved = nullptr;
     long long *owner = nullptr, *neigh = nullptr, *csr_off = nullptr, *csr_face = nullptr;
     int *bc = nullptr;
@@ -103,8 +104,8 @@ struct mmf_umesh {
         if ((e = face<STAGE_1>(U)) != cudaSuccess) return e;
         if ((e = cell<STAGE_1>(U, R)) != cudaSuccess) return e;
         ++launches;
-        if (arith == MMF_ARITH_FAST) uform_w1_kernel<FastArith><<<grid_for(NF * m.ncells), 256, 0, stream>>>(m, U, R, W, ctrl);
-        else uform_w1_kernel<ExactArith><<<grid_for(NF * m.ncells), 256, 0, stream>>>(m, U, R, W, ctrl);
+        if (arith == MMF_ARITH_FAST) uform_w1_kernel<FastArith><<<grid_for(m.ncells), 256, 0, stream>>>(m, U, R, W, ctrl);
+        else uform_w1_kernel<ExactArith><<<grid_for(m.ncells), 256, 0, stream>>>(m, U, R, W, ctrl);
         if ((e = cudaPeekAtLastError()) != cudaSuccess) return e;
         if ((e = face<STAGE_2>(W)) != cudaSuccess) return e;
         if ((e = cell<STAGE_2>(W, R)) != cudaSuccess) return e;       // R := W2
@@ -197,11 +198,18 @@ int mmf_umesh_create(const mmf_umesh_desc *d, int device, mmf_umesh **out)
     A((void **)&u->S, sb);
     A((void **)&u->aos, sb);
     A((void **)&u->P, sizeof(double) * NF * nf);
-    if (d->arith == MMF_ARITH_FAST) A((void **)&u->rec, sizeof(double) * 6 * n);
+    std::vector<double> inv_vol;
+    if (d->arith == MMF_ARITH_FAST) {
+        A((void **)&u->rec, sizeof(double) * 6 * n);
+        A((void **)&u->inv_vol, sizeof(double) * n);
+        inv_vol.resize(n);
+        for (long long c = 0; c < n; ++c) inv_vol[c] = 1.0 / d->cell_volume[c];
+    }
     A((void **)&u->ctrl, sizeof(Ctrl));
     A((void **)&u->rhs_maxeig, sizeof(double));
     auto H = [&](void *dst, const void *src, size_t b) { if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, u->stream); };
     H(u->vol, d->cell_volume, sizeof(double) * n);
+    if (d->arith == MMF_ARITH_FAST) H(u->inv_vol, inv_vol.data(), sizeof(double) * n);
     H(u->solved, solved.data(), (size_t)n);
     H(u->owner, d->owner, sizeof(long long) * nf);
     H(u->neigh, d->neigh, sizeof(long long) * nf);
@@ -223,6 +231,7 @@ int mmf_umesh_create(const mmf_umesh_desc *d, int device, mmf_umesh **out)
     m.ncells = n;
     m.nfaces = nf;
     m.vol = u->vol;
+    m.inv_vol = u->inv_vol;
     m.solved = u->solved;
     m.owner = u->owner;
     m.neigh = u->neigh;
@@ -247,7 +256,7 @@ int mmf_umesh_destroy(mmf_umesh *u)
     cudaFree(u->vol); cudaFree(u->solved); cudaFree(u->owner); cudaFree(u->neigh); cudaFree(u->area);
     cudaFree(u->normal); cudaFree(u->bc); cudaFree(u->csr_off); cudaFree(u->csr_face);
     cudaFree(u->U); cudaFree(u->R); cudaFree(u->W); cudaFree(u->S); cudaFree(u->aos); cudaFree(u->P);
-    cudaFree(u->ctrl); cudaFree(u->rhs_maxeig); cudaFree(u->rec);
+    cudaFree(u->ctrl); cudaFree(u->rhs_maxeig); cudaFree(u->rec); cudaFree(u->inv_vol);
     if (u->stream) cudaStreamDestroy(u->stream);
     delete u;
     return MMF_OK;

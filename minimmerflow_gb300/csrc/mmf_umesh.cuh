@@ -30,6 +30,7 @@ namespace mmf {
 struct UMesh {
     long long ncells, nfaces;
     const double *vol;            // per cell
+    const double *inv_vol;        // fast arithmetic: 1 / vol per cell (no FP64 division in the kernels)
     const unsigned char *solved;  // per cell
     const long long *owner, *neigh;
     const double *area;           // per face
@@ -239,6 +240,7 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
             }
         }
         const double V = m.vol[c];
+        const double s = IsExact<A>::value ? 0.0 : sc.dt * (solved ? __ldg(m.inv_vol + c) : 0.0);
 #pragma unroll
         for (int k = 0; k < NF; ++k) {
             const long long o = k * n + c;
@@ -249,11 +251,11 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
             } else if (STAGE == STAGE_2) {
                 const double u = __ldg(U + o), w = __ldg(state + o);
                 out[o] = IsExact<A>::value ? 0.75 * u + 0.25 * (w + sc.dt * acc[k] / V)
-                                           : fma(0.25, fma(sc.dt / V, acc[k], w), 0.75 * u);
+                                           : fma(0.25, fma(s, acc[k], w), 0.75 * u);
             } else {
                 const double u = U[o], w = __ldg(state + o);
                 out[o] = IsExact<A>::value ? (1. / 3) * u + (2. / 3) * (w + sc.dt * acc[k] / V)
-                                           : fma(2.0 / 3.0, fma(sc.dt / V, acc[k], w), u * (1.0 / 3.0));
+                                           : fma(2.0 / 3.0, fma(s, acc[k], w), u * (1.0 / 3.0));
             }
         }
     }
@@ -274,11 +276,16 @@ __global__ void __launch_bounds__(256) uform_w1_kernel(UMesh m, const double *U,
     if (ctrl->t + dt > ctrl->t_end) dt = ctrl->t_end - ctrl->t;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->dt = dt;
     const long long n = m.ncells;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < NF * n; i += (long long)gridDim.x * blockDim.x) {
-        const long long c = i % n;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
         if (!m.solved[c]) continue;
-        const double u = __ldg(U + i), r = __ldg(R + i), V = m.vol[c];
-        W[i] = IsExact<A>::value ? u + dt * r / V : fma(dt / V, r, u);
+        const double V = m.vol[c];
+        const double s = IsExact<A>::value ? 0.0 : dt * __ldg(m.inv_vol + c);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            const long long i = k * n + c;
+            const double u = __ldg(U + i), r = __ldg(R + i);
+            W[i] = IsExact<A>::value ? u + dt * r / V : fma(s, r, u);
+        }
     }
 }
 

@@ -120,3 +120,73 @@ def test_sod_order2_runs(orc, mmf, arith):
             assert np.array_equal(U, U_ref)
         else:
             assert rel_err(U, U_ref) <= FAST_RTOL
+
+
+def screen_samples(rng, n, nv, dim):
+    """Cells for the positivity screen: physical states with slopes of random
+    size (face states of both signs), face states placed on the boundary
+    2 rho E = |m|^2 to within 1e-18 .. 1e-2, densities near zero, magnitudes
+    scaled by 2^-300 .. 2^300, momentum at round-off level, exact zeros,
+    infinities and NaNs."""
+    ie = nv - 1
+    nm = nv - 2   # momentum components stored
+    rho = np.exp(rng.uniform(np.log(1e-3), np.log(1e3), n))
+    vel = rng.normal(0.0, 3.0, (n, nm))
+    p = np.exp(rng.uniform(np.log(1e-3), np.log(1e3), n))
+    U = np.empty((n, nv))
+    U[:, 0] = rho
+    U[:, 1:1 + nm] = rho[:, None] * vel
+    U[:, ie] = p / 0.4 + 0.5 * rho * (vel ** 2).sum(axis=1)
+    S = U[:, None, :] * rng.uniform(-2.5, 2.5, (n, dim, nv))
+    kind = rng.integers(0, 8, n)
+    # face state on the boundary: pick the +x face f, set uc = f - sigma/2
+    b = kind == 1
+    f = U[b].copy()
+    m2 = (f[:, 1:1 + nm] ** 2).sum(axis=1)
+    delta = np.exp(rng.uniform(np.log(1e-18), np.log(1e-2), b.sum())) * rng.choice([-1.0, 1.0], b.sum())
+    f[:, ie] = m2 * (1.0 + delta) / (2.0 * f[:, 0])
+    U[b] = f - 0.5 * S[b, 0, :]
+    # density near zero on a face
+    b = kind == 2
+    S[b, 0, 0] = -2.0 * U[b, 0] * (1.0 + rng.choice([-1.0, 1.0], b.sum()) * np.exp(rng.uniform(-40, -2, b.sum())))
+    # magnitudes
+    b = kind == 3
+    sc = np.ldexp(1.0, rng.integers(-300, 300, b.sum()))
+    U[b] *= sc[:, None]
+    S[b] *= sc[:, None, None]
+    # momentum at round-off level, small slopes
+    b = kind == 4
+    U[b, 1:1 + nm] = rng.normal(0.0, 1e-17, (b.sum(), nm))
+    S[b] = U[b, None, :] * rng.uniform(-0.1, 0.1, (b.sum(), dim, nv))
+    S[b, :, 1:1 + nm] = rng.normal(0.0, 1e-17, (b.sum(), dim, nm))
+    # exact zeros
+    b = kind == 5
+    U[b, 1:1 + nm] = 0.0
+    S[b] = 0.0
+    # infinities and NaNs here and there
+    b = np.flatnonzero(kind == 6)[:50]
+    U[b[:25], 0] = np.inf
+    S[b[25:], 0, ie] = np.nan
+    return np.ascontiguousarray(U), np.ascontiguousarray(S)
+
+
+@pytest.mark.parametrize("arith,nv,dim", [("reference", 5, 2), ("reference", 5, 3), ("fast", 5, 2), ("fast", 5, 3),
+                                          ("fast", 4, 2)])
+def test_positivity_screen_matches_fp64(mmf, arith, nv, dim):
+    """The FP32 screen of the positivity fallback either defers to FP64 or
+    gives the FP64 answer, on 400k adversarial cells; it decides almost all
+    physical cells itself."""
+    rng = np.random.default_rng(20261204 + 10 * nv + dim)
+    n = 400_000
+    U, S = screen_samples(rng, n, nv, dim)
+    dec = np.empty(n, dtype=np.int32)
+    ref = np.empty(n, dtype=np.uint8)
+    a = mmf.capi.ARITH_FAST if arith == "fast" else mmf.capi.ARITH_REFERENCE
+    mmf.capi.check(mmf.capi.load().mmf_o2_screen_selftest(a, nv, dim, n, mmf.capi.ptr(U), mmf.capi.ptr(S),
+                                                          mmf.capi.ptr(dec), mmf.capi.ptr(ref)))
+    decided = dec >= 0
+    assert np.array_equal(dec[decided], ref[decided].astype(np.int32))
+    assert set(np.unique(dec)) <= {-1, 0, 1}
+    # both answers occur, and the boundary cases are where the screen defers
+    assert (dec == 1).any() and (dec == 0).any() and (dec == -1).any()
+    assert np.mean(decided) > 0.8
