@@ -55,7 +55,7 @@ __global__ void batch_nonzero(const double *__restrict__ v, long long n, int *fl
 {
     bool nz = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        nz |= (__double_as_longlong(v[i]) << 1) != 0;
+        nz |= (mmf::dbits(v[i]) << 1) != 0;
     if (__any_sync(0xffffffffu, nz) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
@@ -162,7 +162,7 @@ static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
             gp.bc_lo[d] = (d < 2) ? g.bc_lo[d] : MMF_BC_FREE_FLOW;
             gp.bc_hi[d] = (d < 2) ? g.bc_hi[d] : MMF_BC_FREE_FLOW;
         }
-        for (int k = 0; k < NF; ++k) gp.dir_prim[k] = g.dirichlet_prim[k];
+        dirichlet_conservatives(g.dirichlet_prim, gp.dir_cons);
         gp.area = g.h;
         gp.vol = g.h * g.h;
         gp.half_area_per_vol = 0.5 * gp.area / gp.vol;

@@ -52,7 +52,7 @@ __global__ void nonzero_plane_kernel(const double *__restrict__ v, long long n, 
 {
     bool nz = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        nz |= (__double_as_longlong(v[i]) << 1) != 0;
+        nz |= (mmf::dbits(v[i]) << 1) != 0;
     if (__any_sync(0xffffffffu, nz) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
@@ -78,7 +78,7 @@ __global__ void aos_to_soa_band_kernel(const double *__restrict__ aos, double *_
         const long long g = base + i;
 #pragma unroll
         for (int k = 0; k < NF; ++k) soa[k * plane + g] = aos[NF * g + k];
-        nz |= (__double_as_longlong(aos[NF * g + 3]) << 1) != 0;
+        nz |= (mmf::dbits(aos[NF * g + 3]) << 1) != 0;
     }
     if (wflag && __any_sync(0xffffffffu, nz) && (threadIdx.x & 31) == 0) atomicOr(wflag, 1);
 }
@@ -162,7 +162,7 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
         gp.bc_lo[d] = (d < grid->dim) ? grid->bc_lo[d] : MMF_BC_FREE_FLOW;
         gp.bc_hi[d] = (d < grid->dim) ? grid->bc_hi[d] : MMF_BC_FREE_FLOW;
     }
-    for (int k = 0; k < NF; ++k) gp.dir_prim[k] = grid->dirichlet_prim[k];
+    dirichlet_conservatives(grid->dirichlet_prim, gp.dir_cons);
     const double h = grid->h;
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;

@@ -49,7 +49,7 @@ struct GridParams {
     int dim;
     int n[3];
     int bc_lo[3], bc_hi[3];
-    double dir_prim[NF];
+    double dir_cons[NF];   // Dirichlet ghost state (conservative, dirichlet_conservatives)
     double area, vol;
     double half_area_per_vol;   // 0.5 area / vol: the fast arithmetic's stage scale per unit dt
     int chunk;      // rows (2D) / planes (3D) per marching chunk
@@ -131,7 +131,7 @@ __device__ __forceinline__ StepScalars step_scalars(const GridParams &gp, const 
     sc.active = ctrl->active != 0;
     if (STAGE == STAGE_2) {
         // main.cpp:398-402
-        double maxEig = __longlong_as_double((long long)ctrl->maxeig_bits);
+        double maxEig = bitsd((long long)ctrl->maxeig_bits);
         double dt = ctrl->cfl_h / maxEig;
         if (ctrl->t + dt > ctrl->t_end) dt = ctrl->t_end - ctrl->t;
         sc.dt = dt;
@@ -155,12 +155,12 @@ __device__ __forceinline__ void step_bookkeeping(Ctrl *ctrl, const StepScalars &
         // main.cpp:399-404: the step's maxEig, dt and new time, as the reference logs them
         if (ctrl->log) {
             double *e = ctrl->log + 3 * (ctrl->step % ctrl->log_cap);
-            e[0] = __longlong_as_double((long long)ctrl->maxeig_bits);
+            e[0] = bitsd((long long)ctrl->maxeig_bits);
             e[1] = sc.dt;
             e[2] = ctrl->t + sc.dt;
         }
         // main.cpp:505-506; the stage-1 reduction slot is cleared for the next step
-        ctrl->last_maxeig = __longlong_as_double((long long)ctrl->maxeig_bits);
+        ctrl->last_maxeig = bitsd((long long)ctrl->maxeig_bits);
         ctrl->t += sc.dt;
         ctrl->step += 1;
         ctrl->maxeig_bits = 0ull;
@@ -265,27 +265,9 @@ __device__ __forceinline__ void load_record(const StageArgs &sa, const GridParam
     load_state<A, STAGE>(sa, gp, sc, g, r.c);
     const bool ghost = (gx | gy | gz) != 0;
     if (ghost) {
-        if (gx) {
-            const double n[3] = {(double)gx, 0.0, 0.0};
-            double t[A::NVAR];
-            ghost_state<A>(gx < 0 ? gp.bc_lo[0] : gp.bc_hi[0], n, r.c, gp.dir_prim, t);
-#pragma unroll
-            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
-        }
-        if (gy) {
-            const double n[3] = {0.0, (double)gy, 0.0};
-            double t[A::NVAR];
-            ghost_state<A>(gy < 0 ? gp.bc_lo[1] : gp.bc_hi[1], n, r.c, gp.dir_prim, t);
-#pragma unroll
-            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
-        }
-        if (DIM == 3 && gz) {
-            const double n[3] = {0.0, 0.0, (double)gz};
-            double t[A::NVAR];
-            ghost_state<A>(gz < 0 ? gp.bc_lo[2] : gp.bc_hi[2], n, r.c, gp.dir_prim, t);
-#pragma unroll
-            for (int k = 0; k < A::NVAR; ++k) r.c[k] = t[k];
-        }
+        if (gx) ghost_in_place<A>(gx < 0 ? gp.bc_lo[0] : gp.bc_hi[0], 0, gx, r.c, gp.dir_cons);
+        if (gy) ghost_in_place<A>(gy < 0 ? gp.bc_lo[1] : gp.bc_hi[1], 1, gy, r.c, gp.dir_cons);
+        if (DIM == 3 && gz) ghost_in_place<A>(gz < 0 ? gp.bc_lo[2] : gp.bc_hi[2], 2, gz, r.c, gp.dir_cons);
     }
     A::template record<DIM>(r, ghost ? nullptr : status);
 }
@@ -375,7 +357,7 @@ __device__ __forceinline__ void publish_reductions(double lmax, unsigned status,
     lmax = warp_max(lmax);
     if (lane == 0) {
         unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)rhs_maxeig : &ctrl->maxeig_bits;
-        atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+        atomicMax(dst, (unsigned long long)dbits(lmax));
     }
     if (STAGE == STAGE_1) {
         status = __reduce_or_sync(0xffffffffu, status);
@@ -512,7 +494,7 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
         if (lane == 0) {
             unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
                                                            : &sa.ctrl->maxeig_bits;
-            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+            atomicMax(dst, (unsigned long long)dbits(lmax));
         }
         if (STAGE == STAGE_1) {
             status = __reduce_or_sync(0xffffffffu, status);

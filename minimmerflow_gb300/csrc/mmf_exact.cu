@@ -66,7 +66,11 @@ __global__ void pointwise_kernel(int op, long long n, const double *a, const dou
     }
     case OP_BC:                                                         // euler.cpp:261-376
         for (int k = 0; k < NF; ++k) dp[k] = dir_prim ? dir_prim[k] : 0.0;
-        ghost_state<ExactArith>(bc, nrm + 3 * i, ai, dp, oi);
+        {
+            double dc[NF];
+            ExactArith::prim2cons(dp, dc);
+            ghost_state<ExactArith>(bc, nrm + 3 * i, ai, dc, oi);
+        }
         break;
     default: break;
     }

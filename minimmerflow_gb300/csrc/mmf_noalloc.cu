@@ -117,7 +117,7 @@ extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_con
         gp.bc_lo[d] = (d < grid->dim) ? grid->bc_lo[d] : MMF_BC_FREE_FLOW;
         gp.bc_hi[d] = (d < grid->dim) ? grid->bc_hi[d] : MMF_BC_FREE_FLOW;
     }
-    for (int k = 0; k < NF; ++k) gp.dir_prim[k] = grid->dirichlet_prim[k];
+    dirichlet_conservatives(grid->dirichlet_prim, gp.dir_cons);
     const double h = grid->h;
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;

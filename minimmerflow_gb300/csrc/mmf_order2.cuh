@@ -64,7 +64,7 @@ __device__ __forceinline__ double mc_slope(double a, double b, double central)
 // compare like the values they encode
 __device__ __forceinline__ long long abs_bits(double x)
 {
-    return __double_as_longlong(x) & 0x7fffffffffffffffll;
+    return dbits(x) & 0x7fffffffffffffffll;
 }
 
 // Fast arithmetic: the MC slope with its compares, absolute values, minima
@@ -74,12 +74,12 @@ __device__ __forceinline__ long long abs_bits(double x)
 // with a and b of the same sign (|a|, |b| below 1e-154).
 __device__ __forceinline__ double mc_slope_bits(double a, double b, double central)
 {
-    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ia = dbits(a), ib = dbits(b);
     const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
     if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;
-    const long long m2 = __double_as_longlong(twice_exact(__longlong_as_double(ma < mb ? ma : mb)));
+    const long long m2 = dbits(twice_exact(bitsd(ma < mb ? ma : mb)));
     const long long mc = abs_bits(central);
-    return __longlong_as_double((m2 < mc ? m2 : mc) | (ia & (long long)0x8000000000000000ull));
+    return bitsd((m2 < mc ? m2 : mc) | (ia & (long long)0x8000000000000000ull));
 }
 
 // division-free admissibility of a state: rho > 0 and 2 rho E > |m|^2
@@ -95,11 +95,11 @@ __device__ __forceinline__ bool admissible(const double *c)
     }
     // fast: "x > 0" as 0 < bits(x) < bits(+inf) on the integer pipe (NaN fails, as in the compare)
     const long long inf = 0x7ff0000000000000ll;
-    const long long ir = __double_as_longlong(c[0]);
+    const long long ir = dbits(c[0]);
     if (!(ir > 0 && ir <= inf)) return false;
     double m2 = fma(c[2], c[2], c[1] * c[1]);
     if (NV == 5) m2 = fma(c[3], c[3], m2);
-    const long long iq = __double_as_longlong(fma(twice_exact(c[0]), c[NV - 1], -m2));
+    const long long iq = dbits(fma(twice_exact(c[0]), c[NV - 1], -m2));
     return iq > 0 && iq <= inf;
 }
 
@@ -142,7 +142,7 @@ __device__ __forceinline__ bool faces_admissible(const double *uc, const double 
 // magnitudes below 2^-126 flush to 0.  Error < 2^-20 |result| + 2^-126.
 __device__ __forceinline__ float scaled_f32(double x, int emax)
 {
-    const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32);
+    const unsigned hi = (unsigned)((unsigned long long)dbits(x) >> 32);
     const int e = (int)((hi >> 20) & 0x7ff) - emax + 127;
     return e > 0 ? __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3)) : 0.0f;
 }
@@ -168,11 +168,11 @@ __device__ __forceinline__ int screen_faces(const double *uc, const double (*sig
     constexpr int IE = NV - 1;
     int emax = 0;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) emax = max(emax, (int)((__double_as_longlong(uc[k]) >> 52) & 0x7ff));
+    for (int k = 0; k < NV; ++k) emax = max(emax, (int)((dbits(uc[k]) >> 52) & 0x7ff));
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) emax = max(emax, (int)((__double_as_longlong(sig[d][k]) >> 52) & 0x7ff));
+        for (int k = 0; k < NV; ++k) emax = max(emax, (int)((dbits(sig[d][k]) >> 52) & 0x7ff));
     if (emax >= 0x7ff) return -1;   // an infinity or a NaN
     float u[NV], au[NV];
 #pragma unroll
@@ -270,9 +270,9 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
                 const long long wrap = (long long)(gp.n[d] - 1) * stride;
                 load_plain<A>(oa.state, n, s ? g - wrap : g + wrap, u);
             } else {
-                double nrm[3] = {0.0, 0.0, 0.0};
-                nrm[d] = s ? 1.0 : -1.0;
-                ghost_state<A>(s ? gp.bc_hi[d] : gp.bc_lo[d], nrm, uc, gp.dir_prim, u);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) u[k] = uc[k];
+                ghost_in_place<A, true>(s ? gp.bc_hi[d] : gp.bc_lo[d], d, s ? 1 : -1, u, gp.dir_cons);
             }
         }
 #pragma unroll
@@ -417,13 +417,11 @@ __device__ __forceinline__ void load_sides(const GridParams &gp, const double *s
     // ghost across the border of direction gdir on side gh[gdir]: the face it
     // shares with the interior cell is on its side -gh[gdir]; the interior
     // face state is on the interior cell's side gh[gdir]
-    double fs[NV], gs[NV];
+    double gs[NV];
     const double off = gh[gdir] > 0 ? 0.5 : -0.5;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) fs[k] = face_value<A>(uc[k], off, sg[gdir][k]);
-    double nrm[3] = {0.0, 0.0, 0.0};
-    nrm[gdir] = (double)gh[gdir];
-    ghost_state<A>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], nrm, fs, gp.dir_prim, gs);
+    for (int k = 0; k < NV; ++k) gs[k] = face_value<A>(uc[k], off, sg[gdir][k]);
+    ghost_in_place<A, true>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], gdir, gh[gdir], gs, gp.dir_cons);
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
 #pragma unroll
@@ -650,7 +648,7 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
         if (lane == 0) {
             unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)sa.rhs_maxeig
                                                            : &sa.ctrl->maxeig_bits;
-            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+            atomicMax(dst, (unsigned long long)dbits(lmax));
         }
         if (STAGE == STAGE_1) {
             status = __reduce_or_sync(0xffffffffu, status);

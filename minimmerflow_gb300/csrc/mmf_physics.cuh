@@ -20,6 +20,26 @@
 
 namespace mmf {
 
+// Bit patterns of doubles through opaque register moves.  With the
+// compiler's own bit casts, integer tricks on the patterns are folded back
+// into floating-point operations (masking the sign bit becomes an FP64
+// absolute value, a select on compared patterns an FP64 minimum or maximum,
+// an OR-ed sign bit an FP64 copysign), which run on the narrow FP64 pipe of
+// this GPU; behind these moves they stay on the integer pipe.
+__device__ __forceinline__ long long dbits(double x)
+{
+    long long i;
+    asm("mov.b64 %0, %1;" : "=l"(i) : "d"(x));
+    return i;
+}
+
+__device__ __forceinline__ double bitsd(long long i)
+{
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"(i));
+    return x;
+}
+
 constexpr int NF = 5;               // constants.hpp:35
 constexpr double GAMMA = 1.4;       // constants.hpp:55
 
@@ -41,7 +61,7 @@ using CellRec = CellRecV<DIM, NF>;
 struct ExactArith {
     static constexpr int NVAR = NF;
     __host__ __device__ static constexpr int field(int k) { return k; }
-    __device__ __forceinline__ static void dirichlet(const double *dir_prim, double *g);
+    __device__ __forceinline__ static void dirichlet(const double *dir_cons, double *g);
     // utils.cpp:48-63
     __device__ __forceinline__ static void cons2prim(const double *c, double *p)
     {
@@ -149,20 +169,20 @@ __device__ __forceinline__ double rcp_newton(double x)
 // on physical magnitudes, far below 1e308).
 __device__ __forceinline__ double half_ftz(double x)
 {
-    const long long ix = __double_as_longlong(x);
+    const long long ix = dbits(x);
     const long long e = ix & 0x7ff0000000000000ll;
     if (e == 0x7ff0000000000000ll) return x;
-    return __longlong_as_double(e > 0x0010000000000000ll ? ix - 0x0010000000000000ll
+    return bitsd(e > 0x0010000000000000ll ? ix - 0x0010000000000000ll
                                                          : ix & (long long)0x8000000000000000ull);
 }
 
 __device__ __forceinline__ double twice_exact(double x)
 {
-    const long long ix = __double_as_longlong(x);
+    const long long ix = dbits(x);
     const long long e = ix & 0x7ff0000000000000ll;
     if (e == 0x7ff0000000000000ll) return x;
     const long long sign = ix & (long long)0x8000000000000000ull;
-    return __longlong_as_double(e != 0 ? ix + 0x0010000000000000ll : ((ix ^ sign) << 1) | sign);
+    return bitsd(e != 0 ? ix + 0x0010000000000000ll : ((ix ^ sign) << 1) | sign);
 }
 
 // Square root by the coupled Newton iteration on s ~ sqrt(x) and
@@ -180,20 +200,20 @@ __device__ __forceinline__ double sqrt_newton(double x)
     r = fma(r, e, r);
     const double d = fma(-s, s, x);
     s = fma(d, r, s);
-    return (__double_as_longlong(x) == 0ll) ? 0.0 : s;
+    return (dbits(x) == 0ll) ? 0.0 : s;
 }
 
 // max of two non-negative doubles through their bit patterns (integer pipe)
 __device__ __forceinline__ double max_nonneg(double a, double b)
 {
-    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-    return __longlong_as_double(ia > ib ? ia : ib);
+    const long long ia = dbits(a), ib = dbits(b);
+    return bitsd(ia > ib ? ia : ib);
 }
 
 // status bits from the sign / exponent bits (integer pipe): rho < 0, p < 0, NaN
 __device__ __forceinline__ unsigned state_flags(double rho, double p)
 {
-    const long long ir = __double_as_longlong(rho), ip = __double_as_longlong(p);
+    const long long ir = dbits(rho), ip = dbits(p);
     unsigned f = 0;
     if (ir < 0) f |= 1u;
     if (ip < 0) f |= 2u;
@@ -261,37 +281,105 @@ struct FastArithT {
         if (NV == 5) cbc[3] = fma(-2.0 * mn, n[2], c[3]);
         cbc[IE] = c[IE];
     }
-    // Dirichlet ghost (utils.cpp:71-83 of the inflow primitive state)
-    __device__ __forceinline__ static void dirichlet(const double *dir_prim, double *g)
+    // Dirichlet ghost: the inflow state, precomputed (dirichlet_conservatives)
+    __device__ __forceinline__ static void dirichlet(const double *dir_cons, double *g)
     {
-        double c[NF];
-        ExactArith::prim2cons(dir_prim, c);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) g[k] = c[field(k)];
+        for (int k = 0; k < NV; ++k) g[k] = dir_cons[field(k)];
     }
 };
 
 using FastArith = FastArithT<5>;
 using FastArith2DW0 = FastArithT<4>;
 
-__device__ __forceinline__ void ExactArith::dirichlet(const double *dir_prim, double *g)
+__device__ __forceinline__ void ExactArith::dirichlet(const double *dir_cons, double *g)
 {
-    prim2cons(dir_prim, g);   // euler.cpp:366-376
+#pragma unroll
+    for (int k = 0; k < NF; ++k) g[k] = dir_cons[k];   // euler.cpp:366-376, precomputed
+}
+
+// The Dirichlet ghost's conservative state, prim2cons (utils.cpp:71-83) of the
+// inflow primitive state in the reference's operation order, computed once on
+// the host.  Every product and quotient goes through a volatile so that the
+// host compiler cannot fuse a multiply-add: the bits are those of the device's
+// ExactArith::prim2cons (IEEE operations, no contraction).
+inline void dirichlet_conservatives(const double *p, double *c)
+{
+    volatile double c0 = p[0] / p[4];
+    volatile double c1 = c0 * p[1], c2 = c0 * p[2], c3 = c0 * p[3];
+    volatile double t1 = c0 * p[4];
+    volatile double t2 = t1 / (GAMMA - 1.0);
+    volatile double s1 = p[1] * p[1], s2 = p[2] * p[2], s3 = p[3] * p[3];
+    volatile double s12 = s1 + s2;
+    volatile double ss = s12 + s3;
+    volatile double h = 0.5 * c0;
+    volatile double t3 = h * ss;
+    c[0] = c0;
+    c[1] = c1;
+    c[2] = c2;
+    c[3] = c3;
+    c[4] = t2 + t3;
 }
 
 // Ghost state behind a border face (euler.cpp:261-308, 347-376).  'n' is the
-// outward normal of the border face; dir_prim is the Dirichlet primitive state.
+// outward normal of the border face; dir_cons is the Dirichlet conservative
+// state (dirichlet_conservatives).
 template <class A>
-__device__ __forceinline__ void ghost_state(int bc, const double *n, const double *c, const double *dir_prim,
+__device__ __forceinline__ void ghost_state(int bc, const double *n, const double *c, const double *dir_cons,
                                             double *g)
 {
     if (bc == BC_REFLECTING || bc == BC_WALL) {
         A::reflect(n, c, g);
     } else if (bc == BC_DIRICHLET) {
-        A::dirichlet(dir_prim, g);
+        A::dirichlet(dir_cons, g);
     } else {
 #pragma unroll
         for (int k = 0; k < A::NVAR; ++k) g[k] = c[k];
+    }
+}
+
+template <int NV>
+struct StateV {
+    double v[NV];
+};
+
+// ghost_state out of line, every argument by value, for kernels where the
+// ghost branch is rare and its registers would weigh on the common path.
+template <class A>
+__device__ __noinline__ StateV<A::NVAR> ghost_state_ool(int bc, double n0, double n1, double n2, StateV<A::NVAR> c,
+                                                        StateV<NF> dir_cons)
+{
+    const double n[3] = {n0, n1, n2};
+    StateV<A::NVAR> g;
+    ghost_state<A>(bc, n, c.v, dir_cons.v, g.v);
+    return g;
+}
+
+// c := the ghost of c across the border face of outward normal +-e_dir
+// (side); OOL takes the out-of-line ghost_state (the order-2 kernels, whose
+// register budget is tight), else it is inlined (the order-1 marches).
+template <class A, bool OOL = false>
+__device__ __forceinline__ void ghost_in_place(int bc, int dir, int side, double *c, const double *dir_cons)
+{
+    const double s = side < 0 ? -1.0 : 1.0;
+    if (OOL) {
+        StateV<A::NVAR> in;
+        StateV<NF> dc;
+#pragma unroll
+        for (int k = 0; k < A::NVAR; ++k) in.v[k] = c[k];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) dc.v[k] = dir_cons[k];
+        const StateV<A::NVAR> g = ghost_state_ool<A>(bc, dir == 0 ? s : 0.0, dir == 1 ? s : 0.0, dir == 2 ? s : 0.0,
+                                                     in, dc);
+#pragma unroll
+        for (int k = 0; k < A::NVAR; ++k) c[k] = g.v[k];
+    } else {
+        double n[3] = {0.0, 0.0, 0.0};
+        n[dir] = s;
+        double g[A::NVAR];
+        ghost_state<A>(bc, n, c, dir_cons, g);
+#pragma unroll
+        for (int k = 0; k < A::NVAR; ++k) c[k] = g[k];
     }
 }
 

@@ -241,7 +241,7 @@ int mmf_umesh_create(const mmf_umesh_desc *d, int device, mmf_umesh **out)
     m.csr_off = u->csr_off;
     m.csr_face = u->csr_face;
     m.rec = u->rec;
-    for (int k = 0; k < NF; ++k) m.dir_prim[k] = d->dirichlet_prim[k];
+    dirichlet_conservatives(d->dirichlet_prim, m.dir_cons);
     *out = u;
     return MMF_OK;
 }

@@ -39,7 +39,7 @@ struct UMesh {
     const long long *csr_off;     // per cell: [off[c], off[c+1]) into csr_face
     const long long *csr_face;    // face index, negated - 1 when the cell is the owner
     double *rec;                  // fast arithmetic: per-cell record, 6 planes (u, v, w, p, a, rho H)
-    double dir_prim[NF];
+    double dir_cons[NF];   // Dirichlet ghost state (conservative, dirichlet_conservatives)
 };
 
 // stage state of cell c (materialised planes)
@@ -147,17 +147,25 @@ __global__ void __launch_bounds__(256) uface_kernel(UMesh m, const double *state
                     for (int k = 0; k < 6; ++k) { ro[k] = __ldg(m.rec + k * n + o); rn[k] = __ldg(m.rec + k * n + nb); }
                 }
             } else {
-                double n2[3] = {nrm[0], nrm[1], nrm[2]};
-                double *fluid = os ? co : cn, *virt = os ? cn : co;
-                if (!os) { n2[0] = -1. * n2[0]; n2[1] = -1. * n2[1]; n2[2] = -1. * n2[2]; }
+                // the fluid side's state and its ghost, placed by selects (no
+                // run-time pointer into the local arrays, which would move
+                // them to local memory); the ghost is computed out of line
                 const long long fc = os ? o : nb;
-                uload(state, n, fc, fluid);
-                ghost_state<ExactArith>(bc, n2, fluid, m.dir_prim, virt);
+                StateV<NF> fl, dp;
+                uload(state, n, fc, fl.v);
+#pragma unroll
+                for (int k = 0; k < NF; ++k) dp.v[k] = m.dir_cons[k];
+                const double sgn = os ? 1.0 : -1.0;   // the ghost faces the fluid cell
+                const StateV<NF> gv = ghost_state_ool<ExactArith>(bc, sgn * nrm[0], sgn * nrm[1], sgn * nrm[2], fl, dp);
+#pragma unroll
+                for (int k = 0; k < NF; ++k) { co[k] = os ? fl.v[k] : gv.v[k]; cn[k] = os ? gv.v[k] : fl.v[k]; }
                 if (!IsExact<A>::value) {
-                    double *rf = os ? ro : rn, *rv = os ? rn : ro;
+                    double rf[6], rv[6];
 #pragma unroll
                     for (int k = 0; k < 6; ++k) rf[k] = __ldg(m.rec + k * n + fc);
-                    fast_record(virt, rv);
+                    fast_record(gv.v, rv);
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) { ro[k] = os ? rf[k] : rv[k]; rn[k] = os ? rv[k] : rf[k]; }
                 }
             }
             const double ar = __ldg(m.area + f);
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(256) uface_kernel(UMesh m, const double *state
         lmax = warp_max(lmax);
         if ((threadIdx.x & 31) == 0) {
             unsigned long long *dst = (STAGE == STAGE_RHS) ? (unsigned long long *)rhs_maxeig : &ctrl->maxeig_bits;
-            atomicMax(dst, (unsigned long long)__double_as_longlong(lmax));
+            atomicMax(dst, (unsigned long long)dbits(lmax));
         }
     }
 }
@@ -201,7 +209,7 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
             sc.dt = ctrl->dt;
         }
         if (STAGE == STAGE_3 && sc.active && blockIdx.x == 0 && threadIdx.x == 0) {
-            ctrl->last_maxeig = __longlong_as_double((long long)ctrl->maxeig_bits);
+            ctrl->last_maxeig = bitsd((long long)ctrl->maxeig_bits);
             ctrl->t += sc.dt;
             ctrl->step += 1;
             ctrl->maxeig_bits = 0ull;
@@ -222,7 +230,7 @@ __global__ void __launch_bounds__(256) ucell_kernel(UMesh m, const double *P, co
             const double m2 = fma(u[3], u[3], fma(u[2], u[2], u[1] * u[1]));
             const double q = fma(twice_exact(u[0]), u[4], -m2);
             // compares on the bit patterns (integer pipe): rho > 0, q NaN
-            const long long ir = __double_as_longlong(u[0]), iq = __double_as_longlong(q);
+            const long long ir = dbits(u[0]), iq = dbits(q);
             status |= state_flags(u[0], (ir > 0 && ir <= 0x7ff0000000000000ll) ? q : 0.0);
             if ((iq & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) status |= 4u;
         }
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(256) uform_w1_kernel(UMesh m, const double *U,
 {
     const bool active = ctrl->active != 0;
     if (!active) return;
-    const double maxEig = __longlong_as_double((long long)ctrl->maxeig_bits);
+    const double maxEig = bitsd((long long)ctrl->maxeig_bits);
     double dt = ctrl->cfl_h / maxEig;
     if (ctrl->t + dt > ctrl->t_end) dt = ctrl->t_end - ctrl->t;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->dt = dt;
