@@ -40,19 +40,26 @@ STAGE_BYTES = {1: 80, 2: 120, 3: 120}
 # 2D slopes read 40 + write 80; 3D slopes read 40 + write 120
 STAGE_BYTES_O2 = {2: {1: 120 + 160, 2: 120 + 120 + 240, 3: 120 + 200},
                   3: {1: 160 + 200, 2: 120 + 160 + 280, 3: 160 + 240}}
-FP64_OPS_PER_CELL_STAGE = None  # filled from the kernel model below (fast arithmetic, 2D)
 
 
 def fp64_ops_per_cell_update_2d():
     """Algorithmic FP64 instructions per cell-update of the fast 2D kernel with
     zero z-momentum (four stored fields), counted from the source per cell and
-    stage: record 28 (reciprocal 3 + MUFU seed, velocities 2, rho|u|^2 2, p 2,
-    sound speed 9 with the MUFU seed, E+p 1, fluxes 5, wave speeds 2), two faces
-    2 x 12, accumulation 12, then the stage update (0, 8, 12) and the stage-2
-    input state (0, 4, 0): 64 + (0, 12, 12) per stage.  The halo lanes and halo
-    rows the kernel also evaluates are not counted (they are overhead, not
-    work of the algorithm)."""
-    return 3 * 64 + 24
+    stage: record 25 (reciprocal 3, velocities 2, rho|u|^2 2, p 2, gamma p / rho
+    2, square root 6, E + p 1, fluxes 5, wave speeds 2; the two MUFU seeds and
+    the halving of the square-root seed are not FP64 instructions), two faces
+    2 x 12, accumulation 12: 61 per stage, plus the stage-2 input state 4 and
+    update 8, and the stage-3 update 12: 61 + 73 + 73.  ncu's per-opcode counts
+    (DADD + DFMA + DMUL) agree: 68.1 + 81.6 + 80.2 per output cell, which also
+    holds the halo lanes (32/30) and each chunk's extra row (21/20);
+    ISSUED_FP64_PER_CELL_UPDATE."""
+    return 61 + 73 + 73
+
+
+# ncu per-opcode FP64 instruction counts per output cell of the three stage
+# launches on the 1024^2 benchmark mesh (profiles/stage2d_fast_sod1024.md):
+# the algorithm plus the halo lanes and rows the decomposition evaluates
+ISSUED_FP64_PER_CELL_UPDATE = 68.1 + 81.6 + 80.2
 
 
 def read_peaks():
@@ -695,7 +702,10 @@ def main():
                  "peak_mixed_ops_per_s": fp64_peak_mixed,
                  "frac_of_mixed": fp64_ops * r["value"] / world / fp64_peak_mixed if fp64_ops else None,
                  "peak_mixed_source": ("measured rate of DADD, DMUL and DFMA whose operands change from one "
-                                       "instruction to the next (probe)")},
+                                       "instruction to the next (probe)"),
+                 "issued_ops_per_cell_update_ncu": ISSUED_FP64_PER_CELL_UPDATE if fp64_ops else None,
+                 "issued_frac_of_mixed": (ISSUED_FP64_PER_CELL_UPDATE * r["value"] / world / fp64_peak_mixed
+                                          if fp64_ops else None)},
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],
         "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,

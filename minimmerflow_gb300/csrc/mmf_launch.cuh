@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mmf_cartesian.cuh"
 #include "mmf_order2.cuh"
 
@@ -104,7 +106,9 @@ inline cudaError_t launch_o2(int op, int stage, const GridParams &gp, const Stag
         }
         return cudaPeekAtLastError();
     case O2_FORM_W1:
-        form_w1_kernel<A><<<elementwise_blocks((long long)A::NVAR * gp.plane), 256, 0, s>>>(gp, sa, W1);
+        // four blocks per SM: each thread divides once for dt (an FP64 division
+        // sequence), so fewer threads, each with more cells
+        form_w1_kernel<A><<<std::min(elementwise_blocks(gp.plane), 4u * 152u), 256, 0, s>>>(gp, sa, W1);
         return cudaPeekAtLastError();
     case O2_STAGE:
         switch (stage) {
