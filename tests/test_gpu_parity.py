@@ -367,3 +367,35 @@ def test_step_log_matches_the_reference_loop(orc, mmf, order):
     np.testing.assert_array_equal(log[:, 0], mel[4:12])
     np.testing.assert_array_equal(log[:, 1], dtl[4:12])
     np.testing.assert_array_equal(log[:, 2], t_ref[5:13])
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_cartesian_dirichlet_inflow_channel(orc, mmf, arith):
+    """A channel with the forward-facing step's Dirichlet inflow on x-lo,
+    free flow on x-hi and reflecting walls in y (problem.cpp:404-438) on the
+    Cartesian kernels: the Dirichlet ghost state the host precomputes with the
+    reference's operation order gives the oracle's bits (reference
+    arithmetic) and stays within 1e-12 (fast)."""
+    from minimmerflow_gb300.solver import CartesianEuler
+    P = mmf.problem
+    n, length = (48, 16), 3.0
+    lo = [P.BC_DIRICHLET, P.BC_REFLECTING, P.BC_FREE_FLOW]
+    hi = [P.BC_FREE_FLOW, P.BC_REFLECTING, P.BC_FREE_FLOW]
+    m = orc.OracleMesh(P.FFSTEP, 2, n, (0.0, 0.0, 0.0), length, bc_lo=lo, bc_hi=hi)
+    rng = np.random.default_rng(11)
+    U0 = m.initial_state()
+    U0 *= 1.0 + 0.05 * rng.standard_normal((m.ncells, 1))
+    U0[:, 3] = 0.0
+    U_ref, t_ref, steps_ref = m.run(U0, 0.5, max_steps=20)
+    with CartesianEuler(2, n, (0.0, 0.0, 0.0), length / n[0], lo, hi, arith=arith,
+                        dirichlet_prim=(1.0, 3.0, 0.0, 0.0, 1.0 / 1.4)) as s:
+        U, t, steps = s.run(U0, 0.5, max_steps=20)
+    assert steps == steps_ref == 20
+    if arith == "reference":
+        assert t == t_ref
+        assert np.array_equal(U, U_ref)
+    else:
+        assert abs(t - t_ref) <= 1e-12 * t_ref
+        assert rel_err(U, U_ref) <= FAST_RTOL
+    # the inflow enters: the first column moves towards the Dirichlet state
+    assert np.abs(U[:, 1] - U0[:, 1]).max() > 0.0
