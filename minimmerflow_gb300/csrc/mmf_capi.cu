@@ -761,7 +761,8 @@ static int pipeline_resources(mmf_ctx *c)
 
 static bool pipeline_applies(const mmf_ctx *c, const double *aos, int64_t n_steps)
 {
-    if (c->grid.order != 1 || c->raw_to_cell || n_steps < 1) return false;
+    // the learned indicator reads the whole state before the slopes: no bands
+    if (c->raw_to_cell || n_steps < 1 || (c->grid.order == 2 && c->indicator)) return false;
     const BandPlan p = band_plan(c);
     if (p.K < 2 || p.K > mmf_ctx::MAX_BANDS) return false;
     cudaPointerAttributes a;
@@ -778,6 +779,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
     const long long plane = gp.plane;
     const bool periodic_slow = (gp.dim == 2 ? gp.bc_lo[1] : gp.bc_lo[2]) == BC_PERIODIC;
     const bool check_w = gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST;
+    const bool o2 = c->grid.order == 2;
     const int K = p.K;
     auto band_cells = [&](int b, long long &base, long long &count) {
         const int r0 = b * p.rows, r1 = std::min(p.n_slow, r0 + p.rows);
@@ -785,6 +787,48 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
         count = (long long)(r1 - r0) * p.slab;
     };
     auto tr_blocks = [](long long count) { return (unsigned)std::min<long long>((count + 255) / 256, 4L * 152); };
+    // stage 1 over the chunks of 'g' (order 2: with the slopes of its rows and
+    // of the rows on both sides already computed)
+    auto stage1 = [&](const GridParams &g, cudaStream_t s) {
+        return o2 ? c->o2_gp(O2_STAGE, STAGE_1, g, c->U, c->R, nullptr, s, 0, 0)
+                  : c->stage_gp(STAGE_1, g, c->U, c->R, s);
+    };
+    // order 2: the stage-1 slopes (and the limiter activity) of rows [r0, r1)
+    auto slopes1 = [&](int r0, int r1, cudaStream_t s) {
+        return c->o2_gp(O2_SLOPES, STAGE_1, c->gp, c->U, nullptr, c->lim_active, s, (long long)r0 * p.slab,
+                        (long long)r1 * p.slab);
+    };
+    // the whole-grid stages on the context stream
+    auto whole_stage1 = [&]() -> cudaError_t {
+        if (!o2) return c->stage(STAGE_1, c->U, c->R);
+        cudaError_t e = c->o2(O2_SLOPES, STAGE_1, c->U, nullptr, c->lim_active);
+        return e == cudaSuccess ? c->o2(O2_STAGE, STAGE_1, c->U, c->R, nullptr) : e;
+    };
+    auto whole_stage2 = [&]() -> cudaError_t {
+        if (!o2) return c->stage(STAGE_2, c->U, c->W);
+        cudaError_t e = c->o2(O2_FORM_W1, STAGE_2, c->U, c->W, nullptr);
+        if (e == cudaSuccess) e = c->o2(O2_SLOPES, STAGE_2, c->W, nullptr, nullptr);
+        return e == cudaSuccess ? c->o2(O2_STAGE, STAGE_2, c->W, c->R, nullptr) : e;
+    };
+    auto whole_stage3 = [&]() -> cudaError_t {
+        if (!o2) return c->stage(STAGE_3, c->U, c->U);
+        cudaError_t e = c->o2(O2_SLOPES, STAGE_3, c->R, nullptr, nullptr);
+        return e == cudaSuccess ? c->o2(O2_STAGE, STAGE_3, c->R, c->U, nullptr) : e;
+    };
+    // the download of band b after its stage 3, on stream bs
+    auto download_band = [&](int b, cudaStream_t bs) -> cudaError_t {
+        long long base, count;
+        band_cells(b, base, count);
+        soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, bs>>>(c->U, c->aos, base, count, plane);
+        ++c->launches;
+        cudaError_t e = cudaPeekAtLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_dn[b], bs);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->ev_dn[b], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(aos + NF * base, c->aos + NF * base, sizeof(double) * NF * count,
+                                cudaMemcpyDeviceToHost, c->copy_stream);
+        return e;
+    };
 
     // upload and transposition, band by band; the device buffers are free once
     // the work enqueued before this call has run
@@ -816,18 +860,34 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
         MMF_CUDA(cudaMemcpyAsync(c->h_flag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->copy_stream));
         MMF_CUDA(cudaEventRecord(c->ev_flag, c->copy_stream));
     }
-    // stage 1 chunk by chunk as soon as the rows it reads are on the device:
+    // Stage 1 chunk by chunk as soon as the rows it reads are on the device:
     // once bands 0..b are transposed (rows below r_b), the chunks whose top
     // neighbour row is below r_b run (on band b's stream); chunk 0 of a
-    // periodic slow axis reads the last row and waits for the last band
+    // periodic slow axis reads the last row and waits for the last band.
+    // Order 2 first computes the slopes of band b's rows (they read one row
+    // on each side, so they wait for band b + 1), and a stage-1 chunk also
+    // reads the slopes of the rows on both sides (band b - 1's last row).
     {
         const int nch = (p.n_slow + p.chunk - 1) / p.chunk;
         int next = periodic_slow ? 1 : 0;   // first chunk not yet launched
         for (int b = 0; b < K; ++b) {
-            const int rb = std::min(p.n_slow, (b + 1) * p.rows);
+            cudaStream_t bs = c->band_stream[b];
+            const int r0 = b * p.rows, rb = std::min(p.n_slow, (b + 1) * p.rows);
             int upto = (b == K - 1) ? nch : (rb - 1) / p.chunk;   // chunks [next, upto) are ready
             const bool first0 = periodic_slow && b == K - 1;
-            MMF_CUDA(cudaStreamWaitEvent(c->band_stream[b], c->ev_tr[b], 0));
+            if (o2) {
+                MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_tr[std::min(b + 1, K - 1)], 0));
+                // a periodic row 0 reads the last row: its slopes come with the last band
+                MMF_CUDA(slopes1(periodic_slow && b == 0 ? 1 : r0, rb, bs));
+                if (periodic_slow && b == K - 1) MMF_CUDA(slopes1(0, 1, bs));
+                // ev_s2b[b]: the slopes of bands 0..b are done (each band's event
+                // follows the previous one's), as the chunks launched here may
+                // reach back more than one band when a band is a single chunk
+                if (b > 0) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2b[b - 1], 0));
+                MMF_CUDA(cudaEventRecord(c->ev_s2b[b], bs));
+            } else {
+                MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_tr[b], 0));
+            }
             if (upto > next || first0) {
                 GridParams g = c->gp;
                 g.chunk = p.chunk;
@@ -835,16 +895,16 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
                 if (upto > next) {
                     g.chunk0 = next;
                     g.nchunk = upto - next;
-                    MMF_CUDA(c->stage_gp(STAGE_1, g, c->U, c->R, c->band_stream[b]));
+                    MMF_CUDA(stage1(g, bs));
                     next = upto;
                 }
                 if (first0) {
                     g.chunk0 = 0;
                     g.nchunk = 1;
-                    MMF_CUDA(c->stage_gp(STAGE_1, g, c->U, c->R, c->band_stream[b]));
+                    MMF_CUDA(stage1(g, bs));
                 }
             }
-            MMF_CUDA(cudaEventRecord(c->ev_s1[b], c->band_stream[b]));
+            MMF_CUDA(cudaEventRecord(c->ev_s1[b], bs));
         }
     }
     for (int q = 0; q < K; ++q) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_s1[q], 0));
@@ -861,20 +921,36 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             if (redo) {
                 MMF_CUDA(cudaMemsetAsync(&c->ctrl->maxeig_bits, 0, sizeof(unsigned long long), c->stream));
                 MMF_CUDA(cudaMemsetAsync(&c->ctrl->status, 0, sizeof(unsigned), c->stream));
-                MMF_CUDA(c->stage(STAGE_1, c->U, c->R));
+                MMF_CUDA(whole_stage1());
             }
         }
     }
     for (int64_t s = 0; s < n_steps; ++s) {
-        if (s > 0) MMF_CUDA(c->stage(STAGE_1, c->U, c->R));
+        if (s > 0) MMF_CUDA(whole_stage1());
         if (s + 1 < n_steps) {
-            MMF_CUDA(c->stage(STAGE_2, c->U, c->W));
-            MMF_CUDA(c->stage(STAGE_3, c->U, c->U));
+            MMF_CUDA(whole_stage2());
+            MMF_CUDA(whole_stage3());
             continue;
         }
-        // last step: stage 2 band by band once stage 1 is done everywhere (dt),
-        // stage 3 of a band once stage 2 is done on its rows and the two
-        // neighbour rows, then its transposition and its download
+        if (o2) {
+            // last step, order 2: stage 2 and the stage-3 slopes on the whole
+            // grid, then stage 3 band by band (a band reads W2 and the slopes
+            // only, and writes U of its own cells), each followed by its
+            // download, on two streams taken in turn
+            MMF_CUDA(whole_stage2());
+            MMF_CUDA(c->o2(O2_SLOPES, STAGE_3, c->R, nullptr, nullptr));
+            MMF_CUDA(cudaEventRecord(c->ev_s2, c->stream));
+            for (int b = 0; b < K; ++b) {
+                cudaStream_t bs = s3_stream(c, b);
+                if (b < S3_STREAMS) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2, 0));
+                MMF_CUDA(c->o2_gp(O2_STAGE, STAGE_3, band_params(c, p, b, b == K - 1), c->R, c->U, nullptr, bs, 0, 0));
+                MMF_CUDA(download_band(b, bs));
+            }
+            continue;
+        }
+        // last step, order 1: stage 2 band by band once stage 1 is done
+        // everywhere (dt), stage 3 of a band once stage 2 is done on its rows
+        // and the two neighbour rows, then its transposition and its download
         MMF_CUDA(cudaEventRecord(c->ev_s2, c->stream));   // stage 1 done
         for (int b = 0; b < K; ++b) {
             cudaStream_t bs = s2_stream(c, b);
@@ -913,15 +989,7 @@ static int advance_host_pipelined(mmf_ctx *c, double *aos, int64_t n_steps, doub
             for (int q = 0; q < K; ++q)
                 if (last || (dep[b] & (1u << q))) MMF_CUDA(cudaStreamWaitEvent(bs, c->ev_s2b[q], 0));
             MMF_CUDA(c->stage_gp(STAGE_3, band_params(c, p, b, last), c->U, c->U, bs));
-            long long base, count;
-            band_cells(b, base, count);
-            soa_to_aos_band_kernel<<<tr_blocks(count), 256, 0, bs>>>(c->U, c->aos, base, count, plane);
-            ++c->launches;
-            MMF_CUDA(cudaPeekAtLastError());
-            MMF_CUDA(cudaEventRecord(c->ev_dn[b], bs));
-            MMF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_dn[b], 0));
-            MMF_CUDA(cudaMemcpyAsync(aos + NF * base, c->aos + NF * base, sizeof(double) * NF * count,
-                                     cudaMemcpyDeviceToHost, c->copy_stream));
+            MMF_CUDA(download_band(b, bs));
         }
     }
     for (int b = 0; b < K; ++b) MMF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_dn[b], 0));

@@ -71,14 +71,23 @@ struct mmf_ctx {
     }
     cudaError_t o2(int op, int st, const double *state, double *out, unsigned char *active)
     {
+        return o2_gp(op, st, gp, state, out, active, stream, 0, gp.plane);
+    }
+    // an order-2 operation with the decomposition 'g' (stage launches over its
+    // chunks) and, for the slopes, the grid cells [cell0, cell1), on stream 'on'
+    cudaError_t o2_gp(int op, int st, const GridParams &g, const double *state, double *out, unsigned char *active,
+                      cudaStream_t on, long long cell0, long long cell1)
+    {
         StageArgs sa;
         sa.U = U; sa.R = R; sa.W = W; sa.out = out; sa.ctrl = ctrl; sa.rhs_maxeig = rhs_maxeig;
         O2Args oa;
         oa.state = state; oa.S = Sl; oa.flag = lim_flag; oa.active = active; oa.limit_mode = limit_mode;
         oa.ctrl = ctrl; oa.stage = st;
+        oa.cell0 = cell0;
+        oa.cell1 = cell1;
         ++launches;
-        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_o2_fast(op, st, gp, sa, oa, W, stream, w_zero)
-                                                                : mmf::launch_o2_exact(op, st, gp, sa, oa, W, stream);
+        return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_o2_fast(op, st, g, sa, oa, W, on, w_zero)
+                                                                : mmf::launch_o2_exact(op, st, g, sa, oa, W, on);
     }
     cudaError_t rk_step()
     {

@@ -99,9 +99,9 @@ inline cudaError_t launch_o2(int op, int stage, const GridParams &gp, const Stag
 {
     switch (op) {
     case O2_SLOPES:
-        if (gp.dim == 2) slopes_kernel<A, 2><<<elementwise_blocks(gp.plane), 256, 0, s>>>(gp, oa);
+        if (gp.dim == 2) slopes_kernel<A, 2><<<elementwise_blocks(oa.cell1 - oa.cell0), 256, 0, s>>>(gp, oa);
         else {
-            if constexpr (HAS3D) slopes_kernel<A, 3><<<elementwise_blocks(gp.plane), 256, 0, s>>>(gp, oa);
+            if constexpr (HAS3D) slopes_kernel<A, 3><<<elementwise_blocks(oa.cell1 - oa.cell0), 256, 0, s>>>(gp, oa);
             else return cudaErrorInvalidValue;
         }
         return cudaPeekAtLastError();

@@ -42,6 +42,7 @@ struct O2Args {
     int limit_mode;
     Ctrl *ctrl;
     int stage;               // 0 = residual-only call, 1..3 = RK stage
+    long long cell0, cell1;  // slopes of grid cells [cell0, cell1) (a band of rows or planes)
 };
 
 // a*b <= 0 -> 0; else sign(a) min(2|a|, 2|b|, |a+b|/2)  (oracle orc_compute_polynomials)
@@ -326,8 +327,7 @@ template <class A, int DIM>
 __global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
 {
     if (!o2_step_active(oa.ctrl, oa.stage)) return;
-    const long long cells = (long long)gp.n[0] * gp.n[1] * gp.n[2];
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < cells;
+    for (long long g = oa.cell0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < oa.cell1;
          g += (long long)gridDim.x * blockDim.x)
         slopes_cell<A, DIM>(gp, oa, g);
 }
@@ -528,11 +528,11 @@ __global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArg
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (warp >= gp.nseg * gp.nchunk) return;
     const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (gp.bookkeep && blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
     if (!sc.active) return;
     double lmax = 0.0;
     unsigned status = 0;
-    march2d_o2<A, STAGE>(gp, sa, state, S, sc, warp % gp.nseg, warp / gp.nseg, lmax, status);
+    march2d_o2<A, STAGE>(gp, sa, state, S, sc, warp % gp.nseg, gp.chunk0 + warp / gp.nseg, lmax, status);
     publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }
 
@@ -554,14 +554,14 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
-    if (blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (gp.bookkeep && blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
     if (!sc.active) return;
 
     const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
     int b = blockIdx.x;
     const int seg = b % gp.nseg; b /= gp.nseg;
     const int rb = b % gp.nrowblk; b /= gp.nrowblk;
-    const int chunk = b;
+    const int chunk = gp.chunk0 + b;
     const int x = seg * SEG - 1 + lane;
     const int y = rb * (BY - 2) - 1 + w;
     const int z0 = chunk * gp.chunk;

@@ -1,10 +1,10 @@
 """GPU: mmf_advance_host with page-locked host buffers runs the banded
-pipeline (uploads overlapping stage 1; with one step per call, stages 2 and
-3 band by band behind stage 1 with the step's maxEig from a record pass;
-downloads overlapping stage 3).  It must give the same bits as the
+pipeline (uploads overlapping stage 1 and, at order 2, its slopes; the last
+step's stage 3 band by band, after a banded stage 2 at order 1; downloads
+overlapping stage 3).  It must give the same bits as the
 unpipelined round trip (pageable buffers: upload, graph-replayed steps,
-download), for both arithmetics, periodic and transmissive slow axes, bands
-as thin as one marching chunk, one and several steps per call, a 2D state
+download), for both arithmetics and orders, periodic and transmissive slow
+axes, bands as thin as one marching chunk, one and several steps per call, a 2D state
 whose z-momentum is not zero after calls where it was (the stage-1 redo), a
 run that reaches its end time, and the per-step log."""
 import dataclasses
@@ -21,9 +21,9 @@ def pinned(shape):
     return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
 
 
-def round_trips(case, arith, states, steps, pin):
+def round_trips(case, arith, states, steps, pin, order=1):
     outs = []
-    with case.solver(arith=arith) as s:
+    with case.solver(arith=arith, order=order) as s:
         s.time_setup(case.cfl, 0.0, math.inf, 10 ** 6)
         for U in states:
             h = pinned(U.shape) if pin else np.empty_like(U)
@@ -54,12 +54,13 @@ CASES = {
 @pytest.mark.parametrize("name", sorted(CASES))
 @pytest.mark.parametrize("arith", ["reference", "fast"])
 @pytest.mark.parametrize("steps", [1, 3])
-def test_pipelined_round_trip_is_bitwise(mmf, name, arith, steps):
+@pytest.mark.parametrize("order", [1, 2])
+def test_pipelined_round_trip_is_bitwise(mmf, name, arith, steps, order):
     case = CASES[name](mmf.problem)
     U0 = case.initial_state()
     states = [U0, U0]
-    a = round_trips(case, arith, states, steps, pin=False)
-    b = round_trips(case, arith, states, steps, pin=True)
+    a = round_trips(case, arith, states, steps, pin=False, order=order)
+    b = round_trips(case, arith, states, steps, pin=True, order=order)
     for (ua, ta), (ub, tb) in zip(a, b):
         assert ta == tb
         np.testing.assert_array_equal(ua, ub)
@@ -67,7 +68,8 @@ def test_pipelined_round_trip_is_bitwise(mmf, name, arith, steps):
 
 @pytest.mark.parametrize("arith", ["reference", "fast"])
 @pytest.mark.parametrize("steps", [1, 2])
-def test_pipelined_z_momentum_switch(mmf, arith, steps):
+@pytest.mark.parametrize("order", [1, 2])
+def test_pipelined_z_momentum_switch(mmf, arith, steps, order):
     P = mmf.problem
     case = P.radial_sod_2d(512)
     U0 = case.initial_state()
@@ -76,8 +78,8 @@ def test_pipelined_z_momentum_switch(mmf, arith, steps):
     Uw[:, 3] = 1e-3 * rng.standard_normal(len(U0)) * U0[:, 0]
     Uw[:, 4] += 0.5 * Uw[:, 3] ** 2 / Uw[:, 0]
     states = [U0, Uw, U0, Uw]
-    a = round_trips(case, arith, states, steps, pin=False)
-    b = round_trips(case, arith, states, steps, pin=True)
+    a = round_trips(case, arith, states, steps, pin=False, order=order)
+    b = round_trips(case, arith, states, steps, pin=True, order=order)
     for (ua, ta), (ub, tb) in zip(a, b):
         assert ta == tb
         np.testing.assert_array_equal(ua, ub)
@@ -128,3 +130,25 @@ def test_pipelined_step_log(mmf):
         first_b, log_b = s.step_log()
     assert first_a == first_b == 0
     np.testing.assert_array_equal(log_a, log_b)
+
+
+def test_pipelined_order2_limiter_modes(mmf):
+    """Order 2 with the limiter on flagged cells only, and with central slopes
+    on a smooth state: the banded round trip keeps the bits."""
+    P = mmf.problem
+    case = P.vortex(2, 512)
+    U0 = case.initial_state()
+    flags = (np.arange(case.ncells) % 3 == 0).astype(np.uint8)
+    for mode in ("flagged", "none"):
+        outs = []
+        for pin in (False, True):
+            with case.solver(order=2) as s:
+                s.set_limiter(mode, flags if mode == "flagged" else None)
+                s.time_setup(case.cfl, 0.0, math.inf, 10 ** 6)
+                h = pinned(U0.shape) if pin else np.empty_like(U0)
+                h[:] = U0
+                ts = [s.advance_host(h, 1) for _ in range(3)]
+                outs.append((h.copy(), ts, s.limiter_activity()))
+        assert outs[0][1] == outs[1][1]
+        np.testing.assert_array_equal(outs[0][0], outs[1][0])
+        np.testing.assert_array_equal(outs[0][2], outs[1][2])
