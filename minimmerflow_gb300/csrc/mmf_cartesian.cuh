@@ -419,19 +419,28 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
     const bool out = out_row && out_col;
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
                perz = gp.bc_lo[2] == BC_PERIODIC;
+    // rows past the one beyond the grid's last row (the overhang of the last
+    // row block) only take part in the block's barriers
+    const bool idle = y > ny;
     unsigned status = 0;
     unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
     double lmax = 0.0;
 
     RecOf<A, 3> cur, abv;
     double Fzlo[NV], Fzhi[NV], Fa[NV], Fb[NV], acc[NV];
-    if (!halo_lo && !halo_hi) {
+    if (!halo_lo && !halo_hi && !idle) {
         load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, abv, nullptr);
         load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
         const double l = face_dir<A, 3>(abv, cur, 2, Fzlo);
         if (out) lmax = max_nonneg(lmax, l);
     }
     for (int z = z0; z < z1; ++z) {
+        if (idle) {   // the three barriers of a plane
+            __syncthreads();
+            __syncthreads();
+            __syncthreads();
+            continue;
+        }
         if (halo_lo || halo_hi) {
             // halo row: y-face state only (the compiler drops the unused fluxes)
             RecOf<A, 3> h;
