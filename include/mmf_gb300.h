@@ -147,6 +147,10 @@ int mmf_autotune(mmf_ctx *ctx, int trial_steps, int *chunk, int *warps_per_block
  * first one.  No reference counterpart (the reference writes a text log). */
 int mmf_set_step_log(mmf_ctx *ctx, int64_t capacity);
 int mmf_get_step_log(mmf_ctx *ctx, double *out, int64_t max_entries, int64_t *first_step, int64_t *n_entries);
+/* Upload the AoS state, advance up to n_steps steps, download into the same
+ * buffer.  With a page-locked buffer (and no raw-id map or learned indicator)
+ * the copies run in bands overlapped with the stages; the bits are those of
+ * the sequential round trip. */
 int mmf_advance_host(mmf_ctx *ctx, double *aos, int64_t n_raw, int64_t n_steps, double *t_out);
 /* Last step's dt and stage-1 maxEig (the reference logs both, main.cpp:399). */
 int mmf_last_step_info(mmf_ctx *ctx, double *dt, double *max_eig);
