@@ -46,7 +46,7 @@ struct mmf_ctx {
     cudaStream_t tr_stream = nullptr;            // upload transpositions, highest priority
     cudaStream_t band_stream[MAX_BANDS] = {};   // band b at priority b (band 0 first)
     cudaEvent_t ev_up[MAX_BANDS] = {}, ev_tr[MAX_BANDS] = {}, ev_s1[MAX_BANDS] = {}, ev_dn[MAX_BANDS] = {};
-    cudaEvent_t ev_s2b[MAX_BANDS] = {};          // stage 2 of band b done (one-step round trip)
+    cudaEvent_t ev_s2b[MAX_BANDS] = {};          // order 1: stage 2 of band b done; order 2: stage-1 slopes of bands 0..b done
     cudaEvent_t ev_start = nullptr, ev_s2 = nullptr, ev_flag = nullptr;
     int *h_flag = nullptr;
     Ctrl *h_ctrl = nullptr;
