@@ -45,21 +45,21 @@ STAGE_BYTES_O2 = {2: {1: 120 + 160, 2: 120 + 120 + 240, 3: 120 + 200},
 def fp64_ops_per_cell_update_2d():
     """Algorithmic FP64 instructions per cell-update of the fast 2D kernel with
     zero z-momentum (four stored fields), counted from the source per cell and
-    stage: record 25 (reciprocal 3, velocities 2, rho|u|^2 2, p 2, gamma p / rho
-    2, square root 6, E + p 1, fluxes 5, wave speeds 2; the two MUFU seeds and
+    stage: record 24 (reciprocal 3, velocities 2, rho|u|^2 2, p 2, gamma p / rho
+    2, square root 5, E + p 1, fluxes 5, wave speeds 2; the two MUFU seeds and
     the halving of the square-root seed are not FP64 instructions), two faces
-    2 x 12, accumulation 12: 61 per stage, plus the stage-2 input state 4 and
-    update 8, and the stage-3 update 12: 61 + 73 + 73.  ncu's per-opcode counts
-    (DADD + DFMA + DMUL) agree: 68.1 + 81.6 + 80.2 per output cell, which also
+    2 x 12, accumulation 12: 60 per stage, plus the stage-2 input state 4 and
+    update 8, and the stage-3 update 12: 60 + 72 + 72.  ncu's per-opcode counts
+    (DADD + DFMA + DMUL) agree: 66.9 + 80.4 + 79.0 per output cell, which also
     holds the halo lanes (32/30) and each chunk's extra row (21/20);
     ISSUED_FP64_PER_CELL_UPDATE."""
-    return 61 + 73 + 73
+    return 60 + 72 + 72
 
 
 # ncu per-opcode FP64 instruction counts per output cell of the three stage
 # launches on the 1024^2 benchmark mesh (profiles/stage2d_fast_sod1024.md):
 # the algorithm plus the halo lanes and rows the decomposition evaluates
-ISSUED_FP64_PER_CELL_UPDATE = 68.1 + 81.6 + 80.2
+ISSUED_FP64_PER_CELL_UPDATE = 66.9 + 80.4 + 79.0
 
 
 def read_peaks():
