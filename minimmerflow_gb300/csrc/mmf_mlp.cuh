@@ -115,7 +115,6 @@ template <int DIM, class Put>
 __device__ __forceinline__ void cell_features(const double *U, const GridParams &gp, long long g, Put put)
 {
     constexpr int NS = DIM == 3 ? 27 : 9;
-    const int nx = gp.n[0], ny = gp.n[1];
     int x, y, z;
     cell_coords(gp, g, x, y, z);
     if (DIM == 2) z = 0;
