@@ -713,9 +713,9 @@ static BandPlan band_plan(const mmf_ctx *c)
     if (p.n_slow < 64 || p.slab * p.n_slow < (1 << 18)) return p;   // too small to pay
     int K = 8;
     int rows = (p.n_slow + K - 1) / K;
-    int ch;
-    if (gp.dim == 2) ch = std::min(8, rows);   // measured best for 1024^2 and 2048^2 with eight bands
-    else ch = std::min(16, rows);                // measured best for 256^3 (16 against 8, 18 and 32)
+    // measured best: 8 rows for 1024^2 and 2048^2, 8 planes for 256^3 (16.00 ms
+    // per round trip against 16.28 with 16 planes and 16.90 with 4)
+    const int ch = std::min(8, rows);
     rows = (rows + ch - 1) / ch * ch;
     p.K = (p.n_slow + rows - 1) / rows;
     p.rows = rows;
