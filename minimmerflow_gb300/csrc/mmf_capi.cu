@@ -1076,7 +1076,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
         for (int ch : {8, 12, 16, 20, 24, 28, 30, 32, 40, 48, 64})
             for (int w : {1, 2, 4}) cand.emplace_back(ch, w);
     } else {
-        for (int ch : {4, 8, 16, 32, 64}) cand.emplace_back(ch, 0);
+        for (int ch : {4, 6, 8, 12, 14, 16, 24, 32, 64}) cand.emplace_back(ch, 0);
     }
     const int by = c->grid.order == 2 ? BY3D_O2 : BY3D;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
