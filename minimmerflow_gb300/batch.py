@@ -1,7 +1,6 @@
 """Batched solver: many independent 2D cases of uneven size in one persistent
 launch per RK stage (C ABI mmf_batch_*), each case with its own CFL time step."""
 import ctypes as C
-import math
 
 import numpy as np
 

@@ -18,7 +18,6 @@ Keys, with the reference's defaults:
   discretization/time/CFL            (main.cpp:100)
   bodies/<any>/{type=box, xMin..zMax} (body.cpp:49-72)
 """
-import math
 import xml.etree.ElementTree as ET
 from dataclasses import dataclass, field
 

@@ -1,7 +1,6 @@
 """settings.xml, the reference's configuration file, read into a problem case
 (minimmerflow_gb300.settings; problem.cpp:37-211, main.cpp:98-121,
 body.cpp:49-72)."""
-import math
 import os
 
 import pytest
