@@ -325,15 +325,20 @@ int mmf_set_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold);
  * device memory is held by a pool allocator).  No counterpart in the
  * reference.  Inputs and outputs are device pointers: d_cons and d_rhs are
  * AoS double[n][5] in raw order, d_max_eig one double, d_raw_to_cell an
- * optional raw -> grid-cell permutation (NULL = row-major).  Work is queued
- * on 'stream' (a cudaStream_t, NULL = the default stream) on the current
- * device and the call returns without waiting.  The working set lives in a
- * static device array of 2*5*MMF_NOALLOC_MAX_CELLS + 32 doubles (about 5.2 MB)
- * that every GPU which loads the library holds until exit; meshes with more
- * cells are rejected with MMF_ERR_ARG.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race.  Reference arithmetic: the result equals mmf_compute_rhs bit for bit. */
+ * optional raw -> grid-cell map (NULL = row-major).  The grid is checked as
+ * mmf_create checks it; order 1 and MMF_ARITH_REFERENCE only (anything else is
+ * MMF_ERR_UNSUPPORTED).  Work is queued on 'stream' (a cudaStream_t, NULL =
+ * the default stream) on the current device and the call returns without
+ * waiting.  The working set lives in a static device array of
+ * 2*5*MMF_NOALLOC_MAX_CELLS + 32 + MMF_NOALLOC_MAX_CELLS/2 doubles (about
+ * 5.5 MB) that every GPU which loads the library holds until exit; meshes with
+ * more cells are rejected with MMF_ERR_ARG.  The map must be a permutation of
+ * 0..n-1: the GPU checks it, and when it is not, every row of d_rhs and
+ * *d_max_eig are set to NaN (the call has returned by then, so no error code
+ * can report it).  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race.  Reference
+ * arithmetic: the result equals mmf_compute_rhs bit for bit. */
 int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_cons, double *d_rhs, double *d_max_eig,
                             const int64_t *d_raw_to_cell, void *stream);
 

@@ -99,6 +99,31 @@ __global__ void soa_to_aos_band_kernel(const double *__restrict__ soa, double *_
 namespace mmf {
 // Records an error for mmf_last_error() from another translation unit.
 int set_last_error(int code, const char *msg) { return fail(code, msg); }
+
+// Checks of a Cartesian grid description, shared by every entry point that
+// takes one: dimension, cells per direction, border codes (periodic sides
+// paired), cell size, reconstruction order and arithmetic.
+int check_grid(const mmf_grid *grid)
+{
+    if (grid->dim != 2 && grid->dim != 3) return fail(MMF_ERR_ARG, "dim must be 2 or 3");
+    for (int d = 0; d < grid->dim; ++d) {
+        if (grid->n[d] < 1) return fail(MMF_ERR_ARG, "cells per direction must be >= 1");
+        const bool plo = grid->bc_lo[d] == MMF_BC_PERIODIC, phi = grid->bc_hi[d] == MMF_BC_PERIODIC;
+        if (plo != phi) return fail(MMF_ERR_ARG, "periodic borders must be paired");
+        for (int s = 0; s < 2; ++s) {
+            const int bc = s ? grid->bc_hi[d] : grid->bc_lo[d];
+            if (bc != MMF_BC_FREE_FLOW && bc != MMF_BC_REFLECTING && bc != MMF_BC_WALL && bc != MMF_BC_DIRICHLET &&
+                bc != MMF_BC_PERIODIC)
+                return fail(MMF_ERR_ARG, "unknown border condition");
+        }
+    }
+    if (!(grid->h > 0.0)) return fail(MMF_ERR_ARG, "h must be > 0");
+    if (grid->order != 1 && grid->order != 2)   // src/reconstruction.cpp:75-76 exits on any other order
+        return fail(MMF_ERR_UNSUPPORTED, "reconstruction order must be 1 or 2");
+    if (grid->arith != MMF_ARITH_REFERENCE && grid->arith != MMF_ARITH_FAST)
+        return fail(MMF_ERR_ARG, "unknown arithmetic");
+    return MMF_OK;
+}
 // mmf_mlp.cu
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
                           unsigned char *flags, cudaStream_t s);
@@ -127,23 +152,8 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
 {
     if (!grid || !out) return fail(MMF_ERR_ARG, "null argument");
     *out = nullptr;
-    if (grid->dim != 2 && grid->dim != 3) return fail(MMF_ERR_ARG, "dim must be 2 or 3");
-    for (int d = 0; d < grid->dim; ++d) {
-        if (grid->n[d] < 1) return fail(MMF_ERR_ARG, "cells per direction must be >= 1");
-        const bool plo = grid->bc_lo[d] == MMF_BC_PERIODIC, phi = grid->bc_hi[d] == MMF_BC_PERIODIC;
-        if (plo != phi) return fail(MMF_ERR_ARG, "periodic borders must be paired");
-        for (int s = 0; s < 2; ++s) {
-            const int bc = s ? grid->bc_hi[d] : grid->bc_lo[d];
-            if (bc != MMF_BC_FREE_FLOW && bc != MMF_BC_REFLECTING && bc != MMF_BC_WALL && bc != MMF_BC_DIRICHLET &&
-                bc != MMF_BC_PERIODIC)
-                return fail(MMF_ERR_ARG, "unknown border condition");
-        }
-    }
-    if (!(grid->h > 0.0)) return fail(MMF_ERR_ARG, "h must be > 0");
-    if (grid->order != 1 && grid->order != 2)   // src/reconstruction.cpp:75-76 exits on any other order
-        return fail(MMF_ERR_UNSUPPORTED, "reconstruction order must be 1 or 2");
-    if (grid->arith != MMF_ARITH_REFERENCE && grid->arith != MMF_ARITH_FAST)
-        return fail(MMF_ERR_ARG, "unknown arithmetic");
+    int rc = mmf::check_grid(grid);
+    if (rc) return rc;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
         return fail(MMF_ERR_CUDA, "no CUDA device available");

@@ -6,10 +6,12 @@
 //
 // The entry point takes device pointers for its inputs and outputs and keeps
 // its working set -- the structure-of-arrays copy of the state, the residual
-// planes and the max-eigenvalue slot -- in one file-scope device array of
-// 2 * 5 * MMF_NOALLOC_MAX_CELLS + 32 doubles (about 5.2 MB), which every GPU
-// that loads this library holds until the process exits.  No cudaMalloc,
-// cudaFree or allocating library routine is called.
+// planes, a slot block (max eigenvalue, cell-map error count) and one counter
+// per cell for the check of the cell map -- in one file-scope device array of
+// 2 * 5 * MMF_NOALLOC_MAX_CELLS + 32 + MMF_NOALLOC_MAX_CELLS / 2 doubles
+// (about 5.5 MB), which every GPU that loads this library holds until the
+// process exits.  No cudaMalloc, cudaFree or allocating library routine is
+// called.
 //
 // In host code the array's name is only a host-side stand-in, not a device
 // address, so the entry point asks the runtime for the device address with
@@ -18,9 +20,13 @@
 // call should therefore come before any stream capture.
 //
 // Every call shares the array and finds the previous call's contents in it:
-// the max-eigenvalue slot is cleared at the start of each call, and the state
-// and residual planes are fully rewritten.  Calls that overlap on the GPU
-// (on different streams, or from different threads) race on the array.
+// the slot block and the per-cell counters are cleared at the start of each
+// call, and the state and residual planes are fully rewritten when the cell
+// map is a permutation.  When it is not (an entry out of range, a cell named
+// twice, a cell never named), some state rows would keep the previous call's
+// values, so the call writes NaN to every residual row and to the max
+// eigenvalue instead of a result.  Calls that overlap on the GPU (on
+// different streams, or from different threads) race on the array.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -38,31 +44,59 @@ using namespace mmf;
 namespace {
 
 constexpr long long kMaxCells = MMF_NOALLOC_MAX_CELLS;
-constexpr long long kSlot = 2LL * NF * kMaxCells;       // max-eigenvalue slot (256-byte aligned offset)
-static __device__ __align__(256) double g_noalloc_scratch[2 * NF * MMF_NOALLOC_MAX_CELLS + 32];
+constexpr long long kSlot = 2LL * NF * kMaxCells;       // slot block (256-byte aligned offset)
+constexpr long long kCount = kSlot + 32;                 // per-cell counters (int), 256-byte aligned
+static __device__ __align__(256) double g_noalloc_scratch[2 * NF * MMF_NOALLOC_MAX_CELLS + 32 +
+                                                          MMF_NOALLOC_MAX_CELLS / 2];
 
 constexpr int kMaxDevices = 64;
 double *g_scratch_addr[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 
+// AoS raw rows -> SoA grid cells.  With a map, each grid cell's counter
+// counts the raw rows that name it, and entries out of [0, n) count as
+// errors (and are not followed).
 __global__ void noalloc_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, long long n,
-                                   const long long *__restrict__ raw_to_cell)
+                                   const long long *__restrict__ raw_to_cell, int *count,
+                                   unsigned long long *map_err)
 {
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= n) return;
     const long long g = raw_to_cell ? raw_to_cell[r] : r;
-    if (g < 0 || g >= n) return;
+    if (g < 0 || g >= n) {
+        atomicAdd(map_err, 1ull);
+        return;
+    }
+    if (raw_to_cell) atomicAdd(count + g, 1);
 #pragma unroll
     for (int k = 0; k < NF; ++k) soa[k * n + g] = aos[NF * r + k];
 }
 
+// The map is a permutation when every grid cell was named exactly once.
+__global__ void noalloc_check_map(const int *__restrict__ count, long long n, unsigned long long *map_err)
+{
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g < n && count[g] != 1) atomicAdd(map_err, 1ull);
+}
+
+// SoA residual -> AoS raw rows, and the max eigenvalue.  A map that was not
+// a permutation leaves NaN everywhere (rows of cells never named would hold
+// the previous call's state, so no row can be trusted).
 __global__ void noalloc_soa_to_aos(const double *__restrict__ soa, double *__restrict__ aos, long long n,
-                                   const long long *__restrict__ raw_to_cell)
+                                   const long long *__restrict__ raw_to_cell,
+                                   const unsigned long long *__restrict__ map_err, const double *__restrict__ me,
+                                   double *max_eig)
 {
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool bad = *map_err != 0ull;
+    if (r == 0) *max_eig = bad ? __longlong_as_double(0x7ff8000000000000ll) : *me;
     if (r >= n) return;
     const long long g = raw_to_cell ? raw_to_cell[r] : r;
-    if (g < 0 || g >= n) return;
+    if (bad || g < 0 || g >= n) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) aos[NF * r + k] = __longlong_as_double(0x7ff8000000000000ll);
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < NF; ++k) aos[NF * r + k] = soa[k * n + g];
 }
@@ -88,25 +122,26 @@ int scratch_of_current_device(double **out)
 
 } // namespace
 
+namespace mmf {
+int check_grid(const mmf_grid *grid);   // mmf_capi.cu
+}
+
 extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_cons, double *d_rhs,
                                        double *d_max_eig, const int64_t *d_raw_to_cell, void *stream)
 {
     if (!grid || !d_cons || !d_rhs || !d_max_eig) return set_last_error(MMF_ERR_ARG, "null argument");
-    if (grid->dim != 2 && grid->dim != 3) return set_last_error(MMF_ERR_ARG, "dim must be 2 or 3");
+    int rc = mmf::check_grid(grid);
+    if (rc) return rc;
     if (grid->order != 1) return set_last_error(MMF_ERR_UNSUPPORTED, "only order 1 is supported");
-    if (!(grid->h > 0.0)) return set_last_error(MMF_ERR_ARG, "h must be > 0");
+    if (grid->arith != MMF_ARITH_REFERENCE)
+        return set_last_error(MMF_ERR_UNSUPPORTED, "only the reference arithmetic is supported");
     long long n = 1;
-    for (int d = 0; d < grid->dim; ++d) {
-        if (grid->n[d] < 1) return set_last_error(MMF_ERR_ARG, "cells per direction must be >= 1");
-        if ((grid->bc_lo[d] == MMF_BC_PERIODIC) != (grid->bc_hi[d] == MMF_BC_PERIODIC))
-            return set_last_error(MMF_ERR_ARG, "periodic borders must be paired");
-        n *= grid->n[d];
-    }
+    for (int d = 0; d < grid->dim; ++d) n *= grid->n[d];
     if (n > kMaxCells)
         return set_last_error(MMF_ERR_ARG, "mmf_compute_rhs_noalloc: the mesh has more cells than "
                                            "MMF_NOALLOC_MAX_CELLS (65536)");
     double *scratch = nullptr;
-    int rc = scratch_of_current_device(&scratch);
+    rc = scratch_of_current_device(&scratch);
     if (rc) return rc;
 
     GridParams gp;
@@ -126,11 +161,19 @@ extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_con
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double *state = scratch, *rhs = scratch + NF * kMaxCells, *me = scratch + kSlot;
+    unsigned long long *map_err = reinterpret_cast<unsigned long long *>(scratch + kSlot + 1);
+    int *count = reinterpret_cast<int *>(scratch + kCount);
     const long long *map = reinterpret_cast<const long long *>(d_raw_to_cell);
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    cudaError_t e = cudaMemsetAsync(me, 0, sizeof(double), s);
+    // the max-eigenvalue slot and the map error count start at zero
+    cudaError_t e = cudaMemsetAsync(me, 0, 32 * sizeof(double), s);
+    if (e == cudaSuccess && map) e = cudaMemsetAsync(count, 0, sizeof(int) * n, s);
     if (e == cudaSuccess) {
-        noalloc_aos_to_soa<<<blocks, 256, 0, s>>>(d_cons, state, n, map);
+        noalloc_aos_to_soa<<<blocks, 256, 0, s>>>(d_cons, state, n, map, count, map_err);
+        e = cudaPeekAtLastError();
+    }
+    if (e == cudaSuccess && map) {
+        noalloc_check_map<<<blocks, 256, 0, s>>>(count, n, map_err);
         e = cudaPeekAtLastError();
     }
     if (e == cudaSuccess) {
@@ -139,10 +182,9 @@ extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_con
         e = launch_stage_exact(STAGE_RHS, gp, sa, s);
     }
     if (e == cudaSuccess) {
-        noalloc_soa_to_aos<<<blocks, 256, 0, s>>>(rhs, d_rhs, n, map);
+        noalloc_soa_to_aos<<<blocks, 256, 0, s>>>(rhs, d_rhs, n, map, map_err, me, d_max_eig);
         e = cudaPeekAtLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_max_eig, me, sizeof(double), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return set_last_error(MMF_ERR_CUDA, cudaGetErrorString(e));
     return MMF_OK;
 }

@@ -58,4 +58,5 @@ def main(ref_src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    main(sys.argv[1] if len(sys.argv) > 1
+         else os.path.join(os.environ.get("MMF_REFERENCE", "/root/reference"), "src"))

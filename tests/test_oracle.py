@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-REF_SRC = "/root/reference/src"
+REF_SRC = os.path.join(os.environ.get("MMF_REFERENCE", "/root/reference"), "src")
 
 
 @pytest.mark.parametrize("name", ["2dIsentropicVortex", "2dRadSod", "3dIsentropicVortexXY",

@@ -7,7 +7,7 @@ import pytest
 
 import minimmerflow_gb300 as mmf
 
-REF_TESTS = "/root/reference/test"
+REF_TESTS = os.path.join(os.environ.get("MMF_REFERENCE", "/root/reference"), "test")
 
 FFSTEP_XML = """<?xml version="1.0"?>
 <minimmerflow version="1">

@@ -46,13 +46,72 @@ def test_noalloc_rhs_matches_context_rhs(mmf, pname, dim, n, morton):
         assert d_me.item() == me_ref
 
 
-def test_noalloc_rejects_meshes_above_the_maximum(mmf):
-    lib = mmf.capi.load()
-    case = mmf.problem.reference_case("radsod", 2, 512)   # 262144 cells > 65536
+def _grid(mmf, n, h=0.1):
     g = mmf.capi.Grid()
-    g.dim, g.h, g.order, g.arith = 2, case.h, 1, 0
-    g.n[0], g.n[1], g.n[2] = 512, 512, 1
+    g.dim, g.h, g.order, g.arith = 2, h, 1, 0
+    g.n[0], g.n[1], g.n[2] = n, n, 1
+    return g
+
+
+def test_noalloc_rejects_meshes_above_the_maximum(mmf):
+    """Sizes beyond the static array, and what the entry point does not
+    support, are refused before any GPU work is queued (the buffers here are
+    host memory that no kernel ever sees)."""
+    lib = mmf.capi.load()
     buf = (C.c_double * 8)()
+    g = _grid(mmf, 512)   # 262144 cells > 65536
     rc = lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None)
     assert rc == mmf.capi.MMF_ERR_ARG
     assert b"65536" in lib.mmf_last_error()
+    g = _grid(mmf, 16)
+    g.arith = mmf.capi.ARITH_FAST
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_UNSUPPORTED
+    g.arith = 7
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_ARG
+    g = _grid(mmf, 16)
+    g.order = 2
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_UNSUPPORTED
+    g = _grid(mmf, 16)
+    g.bc_lo[1] = 9   # no such border condition
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_ARG
+    assert b"border" in lib.mmf_last_error()
+    g = _grid(mmf, 16, h=0.0)
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_ARG
+
+
+@pytest.mark.parametrize("fault", ["duplicate", "out_of_range"])
+def test_noalloc_map_that_is_not_a_permutation_gives_nan(mmf, fault):
+    """A cell map with a repeated entry leaves a cell that no raw row fills,
+    whose state would be the previous call's; one with an entry outside
+    [0, n) is skipped by the kernels' bounds checks.  Either way the call
+    writes NaN everywhere instead of a residual.  A good call right after
+    gives the exact residual again."""
+    import torch
+    lib = mmf.capi.load()
+    case = mmf.problem.reference_case("radsod", 2, 32)
+    U = case.initial_state()
+    with case.solver(arith="reference") as s:
+        R_ref, me_ref = s.compute_rhs(U)
+        grid = s.grid
+    dev = torch.device("cuda", 0)
+    bad = np.arange(case.ncells, dtype=np.int64)
+    if fault == "duplicate":
+        bad[5] = 6
+    else:
+        bad[5] = case.ncells + 3
+        bad[9] = -1
+    d_u = torch.from_numpy(U).to(dev)
+    d_rhs = torch.zeros((case.ncells, 5), dtype=torch.float64, device=dev)
+    d_me = torch.zeros((1,), dtype=torch.float64, device=dev)
+    for m, expect_nan in [(bad, True), (np.arange(case.ncells, dtype=np.int64), False)]:
+        d_map = torch.from_numpy(m).to(dev)
+        torch.cuda.synchronize()
+        rc = lib.mmf_compute_rhs_noalloc(C.byref(grid), mmf.capi.ptr(d_u), mmf.capi.ptr(d_rhs),
+                                         mmf.capi.ptr(d_me), mmf.capi.ptr(d_map), None)
+        assert rc == 0, lib.mmf_last_error()
+        torch.cuda.synchronize()
+        R = d_rhs.cpu().numpy()
+        if expect_nan:
+            assert np.isnan(R).all() and np.isnan(d_me.item())
+        else:
+            assert np.array_equal(R, R_ref) and d_me.item() == me_ref
