@@ -16,6 +16,19 @@ roofline / fp64: the stage-2 kernel (dominant, 120 B/cell algorithmic) timed
          per launch with events; peaks from MEASURED_PEAKS.json.
 cpu_baseline: the oracle (C restatement, bit-identical to the reference
          sources) on the host cores, on a bounded sample of steps.
+fp64   : the FP64 issue rate measured in this run (mmf_fp64_rate), the bound
+         of the stage kernels, against the algorithm's FP64 instructions.
+The default line also carries (each with its own workload description):
+  vortex3d_256    3D isentropic vortex 256^3, axis z and axis x;
+  batched_learned the 512-case order-2 sweep: batched + learned indicator,
+                  batched with every cell limited and with none limited, the
+                  plain per-case path on concurrent streams and one after
+                  another, one plain grid of the same size; L1 error ratio;
+  sod3d_learned   3D radial Sod 256^3, order 2, learned / plain / unlimited;
+  dropin_binding  the reference loop through three mmf_compute_rhs host calls
+                  per step;
+  sustained       about 1.5 s of back-to-back steps with clock samples;
+  step_times      the spread of the K timed steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -33,6 +46,11 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# The per-case baseline of the batched sweep runs hundreds of contexts on
+# their own streams: give the device more than the default eight hardware
+# work queues, so that streams do not queue behind one another (read once,
+# when CUDA starts in this process).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 CELL_BYTES_STEP = 320          # algorithmic HBM bytes per cell-update (8 x 5 fields x 8 B)
 STAGE_BYTES = {1: 80, 2: 120, 3: 120}
@@ -314,10 +332,211 @@ def run_batched(args, world, rank, local, dist):
                 plain=plain_value, status_bad=status_bad, ncases=len(cases), accuracy=acc)
 
 
-def run_learned(args, world, rank, local, dist):
+def run_sweep_comparison(args, local, steps, warmup):
+    """The 512-case seeded sweep at order 2 (MC limiter), FP64: the batched
+    solver with the learned indicator, without it (every cell limited), and
+    with the limiter off everywhere (central slopes: the most any indicator
+    could save, since an indicator only removes limiter work), against the
+    same cases run by the plain per-case path -- one context per case, all
+    contexts' steps enqueued on their own streams at once so that the GPU
+    overlaps them (a fair plain alternative), and one after another (the
+    sequential figure) -- and against one plain grid of about as many cells
+    as the whole sweep.  Accuracy: the L1 density error of every vortex case
+    against its exact solution after 20 steps, learned over plain."""
+    import torch
+    import minimmerflow_gb300 as mmf
+    from minimmerflow_gb300.batch import BatchEuler
+    from minimmerflow_gb300 import train_indicator
+
+    torch.cuda.set_device(local)
+    cases = mmf.problem.batched_sweep(ncases=args.ncases, seed=args.seed)
+    for c in cases:
+        c.cfl = args.cfl_order2
+    states = [c.initial_state() for c in cases]
+    mlp, thr = train_indicator.load(2, device=local)
+    trained_here = mlp is None
+    if mlp is None:
+        mlp, _, thr = train_indicator.train(2, samples=1_000_000, epochs=8, log=None)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {"cases": len(cases), "cells": int(sum(c.ncells for c in cases)), "threshold": thr,
+           "indicator_trained_in_this_run": trained_here}
+    total = out["cells"]
+
+    b = BatchEuler(cases, arith=args.arith, device=local, order=2)
+    packed = b.pack(states)
+    stream = torch.cuda.ExternalStream(b.stream_handle, device=torch.device("cuda", local))
+    finals = {}
+    for mode in ("learned", "limited", "unlimited"):
+        b.set_indicator(mlp if mode == "learned" else None, thr)
+        if mode == "unlimited":
+            b.set_limiter("none")
+        b.upload(packed)
+        b.time_setup(max_steps=10 ** 9)
+        chunk, bps = b.autotune(trial_steps=2)
+        b.advance_async(warmup)
+        b.synchronize()
+        l0 = b.launch_count
+        durs = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.advance_async(1)
+            e1.record(stream)
+            e1.synchronize()
+            durs.append(e0.elapsed_time(e1) / 1e3)
+        out[mode] = {"value": total * steps / sum(durs), "unit": "cell-updates/s", "step_times": step_stats(durs),
+                     "launches": b.launch_count - l0, "chunk": chunk, "blocks_per_sm": bps}
+        if mode != "unlimited":
+            finals[mode] = (b.run(states, 20), [b.case_info(i)[0] for i in range(len(cases))])
+    b.close()
+    del packed
+
+    # accuracy: vortex cases against the exact solution after 20 steps
+    ratios, el_sum, ep_sum = [], 0.0, 0.0
+    for i, c in enumerate(cases):
+        if c.problem != mmf.problem.VORTEX_XY:
+            continue
+        # each case and each run has its own time after 20 steps (its own dt sequence)
+        ep = c.l1_density_error(finals["limited"][0][i], finals["limited"][1][i])
+        el = c.l1_density_error(finals["learned"][0][i], finals["learned"][1][i])
+        ratios.append(el / ep)
+        el_sum += el
+        ep_sum += ep
+    out["accuracy"] = {"vortex_cases": len(ratios), "steps": 20,
+                       "l1_error_ratio_learned_over_plain": {"mean": float(np.mean(ratios)),
+                                                             "max": float(np.max(ratios)),
+                                                             "sum_over_cases": el_sum / ep_sum},
+                       "plain": "the batched order 2 with every cell limited, bit-identical per case to a "
+                                "single-case context (tests/test_gpu_batch.py)"}
+    del finals
+
+    # plain per-case contexts on concurrent streams, and one after another
+    ctxs = []
+    for c, U0 in zip(cases, states):
+        sv = c.solver(arith=args.arith, device=local, order=2)
+        sv.upload(U0)
+        sv.time_setup(c.cfl, 0.0, math.inf, 10 ** 9)
+        sv.advance(1)
+        ctxs.append(sv)
+    torch.cuda.synchronize()
+    k = max(2, min(steps, 8))
+    best = 0.0
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for sv in ctxs:
+            sv.advance_async(k)
+        torch.cuda.synchronize()
+        best = max(best, total * k / (time.perf_counter() - t0))
+    out["plain_concurrent_streams"] = {
+        "value": best, "unit": "cell-updates/s",
+        "how": "one plain order-2 context per case (every cell limited), %d steps of every context enqueued on "
+               "the contexts' own streams before one device synchronisation, host clock, best of 2; "
+               "CUDA_DEVICE_MAX_CONNECTIONS=%s" % (k, os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"))}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for sv in ctxs:
+        sv.advance(k)
+    torch.cuda.synchronize()
+    out["plain_sequential_contexts"] = {"value": total * k / (time.perf_counter() - t0), "unit": "cell-updates/s",
+                                        "how": "the same contexts run one after another, %d steps each" % k}
+    for sv in ctxs:
+        sv.close()
+    del ctxs, states
+
+    # one plain grid of about the sweep's total cells
+    n1 = int(round(math.sqrt(total)))
+    big = mmf.problem.radial_sod_2d(n=n1)
+    big.cfl = args.cfl_order2
+    with big.solver(arith=args.arith, device=local, order=2) as sv:
+        sv.upload(big.initial_state())
+        sv.time_setup(big.cfl, 0.0, math.inf, 10 ** 9)
+        sv.autotune(trial_steps=2)
+        sv.advance(2)
+        st = torch.cuda.ExternalStream(sv.stream_handle, device=torch.device("cuda", local))
+        durs = []
+        for _ in range(max(2, min(steps, 5))):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            sv.advance_async(1)
+            e1.record(st)
+            e1.synchronize()
+            durs.append(e0.elapsed_time(e1) / 1e3)
+    out["plain_single_grid"] = {"value": n1 * n1 * len(durs) / sum(durs), "unit": "cell-updates/s",
+                                "how": "one %dx%d radial Sod grid (order 2, every cell limited), about the "
+                                       "sweep's total cells" % (n1, n1)}
+    out["learned_over_plain_concurrent"] = out["learned"]["value"] / out["plain_concurrent_streams"]["value"]
+    out["learned_over_batched_limited"] = out["learned"]["value"] / out["limited"]["value"]
+    out["ceiling_unlimited_over_limited"] = out["unlimited"]["value"] / out["limited"]["value"]
+    return out
+
+
+def run_dropin(args, local, steps):
+    """The reference loop (src/main.cpp:377-506) through the minimal drop-in
+    binding: per stage one mmf_compute_rhs call on host buffers (upload of the
+    stage state, the residual on the GPU, download of the residual and maxEig)
+    -- the call the C++ adapter's euler::computeRHS makes -- and the RK
+    updates of the reference loop on the host, in numpy."""
+    import minimmerflow_gb300 as mmf
+
+    case = mmf.problem.radial_sod_2d(n=args.n)
+    U = np.ascontiguousarray(case.initial_state())
+    V = case.h ** 2
+    h = case.h
+    W = np.empty_like(U)
+    tmp = np.empty_like(U)
+    with case.solver(arith="reference", device=local) as s:
+        def step(t):
+            R, me = s.compute_rhs(U)
+            dt = 0.9 * case.cfl * h / me
+            if t + dt > case.t_end:
+                dt = case.t_end - t
+            f = dt / V
+            np.multiply(R, f, out=W)
+            W += U
+            R, _ = s.compute_rhs(W)
+            np.multiply(R, f, out=tmp)
+            tmp += W
+            tmp *= 0.25
+            np.multiply(U, 0.75, out=W)
+            W += tmp
+            R, _ = s.compute_rhs(W)
+            np.multiply(R, f, out=tmp)
+            tmp += W
+            tmp *= 2.0 / 3.0
+            U *= 1.0 / 3.0
+            U += tmp
+            return t + dt
+        t = step(0.0)
+        gpu_s, tot0 = 0.0, time.perf_counter()
+        for _ in range(steps):
+            t = step(t)
+        total_s = time.perf_counter() - tot0
+        # the three residual calls alone (their host copies included)
+        g0 = time.perf_counter()
+        for _ in range(steps):
+            for _ in range(3):
+                s.compute_rhs(U)
+        gpu_s = time.perf_counter() - g0
+    return {"value": case.ncells * steps / total_s, "unit": "cell-updates/s", "steps": steps,
+            "ms_per_step": 1e3 * total_s / steps, "compute_rhs_ms_per_step": 1e3 * gpu_s / steps,
+            "host_rk_ms_per_step": 1e3 * (total_s - gpu_s) / steps,
+            "how": "reference loop with three mmf_compute_rhs calls per step on pageable host buffers "
+                   "(reference arithmetic) and the RK updates in numpy on one host core, %dx%d radial Sod"
+                   % (args.n, args.n)}
+
+
+def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
     """3D radial Sod (order 2, MC limiter) with and without the learned
-    troubled-cell indicator; accuracy against the exact solution on a 3D
-    isentropic vortex with the same two settings."""
+    troubled-cell indicator, and with the limiter off everywhere (the most an
+    indicator could save); accuracy against the exact solution on a 3D
+    isentropic vortex with the first two settings."""
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     import torch
     import minimmerflow_gb300 as mmf
     from minimmerflow_gb300 import indicator, train_indicator
@@ -335,20 +554,22 @@ def run_learned(args, world, rank, local, dist):
     U0 = case.initial_state()
     out = {}
     finals = {}
-    for mode in ("plain", "learned"):
+    for mode in ("plain", "learned", "unlimited"):
         s = case.solver(arith=args.arith, device=local, order=2)
         if mode == "learned":
             indicator.use_indicator(s, mlp, args.threshold)
+        if mode == "unlimited":
+            s.set_limiter("none")
         stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
         s.upload(U0)
         s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
-        s.advance(args.warmup)
+        s.advance(warmup)
         launches0 = s.launch_count
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
         durs = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -358,10 +579,11 @@ def run_learned(args, world, rank, local, dist):
             e1.record(stream)
             e1.synchronize()
             durs.append(e0.elapsed_time(e1) / 1e3)
-        value, total = replica_throughput(sum(durs), case.ncells * args.steps, world, dist)
-        out[mode] = dict(value=value, ms=1e3 * total / args.steps,
-                         launches=s.launch_count - launches0, status=s.status())
-        finals[mode] = s.download()
+        value, total = replica_throughput(sum(durs), case.ncells * steps, world, dist)
+        out[mode] = dict(value=value, ms=1e3 * total / steps,
+                         launches=s.launch_count - launches0, status=s.status(), step_times=step_stats(durs))
+        if mode != "unlimited":
+            finals[mode] = s.download()
         if mode == "learned":
             _, flags = indicator.run_indicator(s, mlp, args.threshold)
             out[mode]["limited_fraction"] = float(flags.mean())
@@ -459,13 +681,25 @@ def run_facelist(args, world, rank, local, dist):
     return dict(value=value, total=total, launches=launches, ncell=case.ncells)
 
 
-def run_ours(args, world, rank, local, dist):
+def step_stats(durs):
+    """Spread of the per-step times of a timed region (ms)."""
+    ms = [1e3 * d for d in durs]
+    return {"n": len(ms), "min_ms": min(ms), "median_ms": statistics.median(ms), "max_ms": max(ms),
+            "stdev_ms": statistics.stdev(ms) if len(ms) > 1 else 0.0}
+
+
+def run_ours(args, world, rank, local, dist, case=None, steps=None, warmup=None, sustained_s=0.0, clocks=True):
+    """One Cartesian context: K timed steps (value), per-stage launch times
+    (roofline), the host round trip (e2e) and, when sustained_s > 0, a
+    sustained run of that many seconds of back-to-back steps."""
     import numpy as np
     import torch
     import minimmerflow_gb300 as mmf
 
     torch.cuda.set_device(local)
-    case = make_case(args)
+    case = make_case(args) if case is None else case
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     U0 = case.initial_state()
     ncell = case.ncells
     s = case.solver(arith=args.arith, device=local, chunk=args.chunk, order=args.order)
@@ -489,7 +723,7 @@ def run_ours(args, world, rank, local, dist):
             restart()
 
     # warm-up
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ensure_room()
         s.advance_async(1)
     s.synchronize()
@@ -515,17 +749,50 @@ def run_ours(args, world, rank, local, dist):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    clk = ClockSampler(local)
-    clk.start()
-    durs = timed_steps(args.steps)
+    clk = ClockSampler(local) if clocks else None
+    if clk:
+        clk.start()
+    durs = timed_steps(steps)
     torch.cuda.synchronize()
-    clocks = clk.stop()
+    clock_rec = clk.stop() if clk else None
     launches = s.launch_count - launches0
-    value, total = replica_throughput(sum(durs), ncell * args.steps, world, dist)
+    value, total = replica_throughput(sum(durs), ncell * steps, world, dist)
+
+    # sustained: back-to-back steps from the step graphs for about sustained_s
+    # seconds, one pair of events around them, clocks sampled meanwhile
+    sustained = None
+    if sustained_s > 0:
+        per = max(1, int(sustained_s / max(min(durs), 1e-6)))
+        per = min(per, 100000)
+        if not math.isinf(case.t_end):
+            restart()   # the run restarts from its initial state outside the events
+        clk2 = ClockSampler(local)
+        clk2.start()
+        done, secs = 0, 0.0
+        while done < per:
+            k = per - done
+            if not math.isinf(case.t_end):
+                # the first 300 steps stay well before t_end (about 520 steps at 1024^2)
+                t_now, st_now = s.time_info()
+                k = min(k, 300 - st_now) if st_now < 300 else 0
+                if k <= 0:
+                    restart()
+                    continue
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.advance_async(k)
+            e1.record(stream)
+            e1.synchronize()
+            secs += e0.elapsed_time(e1) / 1e3
+            done += k
+        sustained = {"steps": done, "seconds": secs, "value": ncell * done / secs, "unit": "cell-updates/s",
+                     "l2": "not flushed (state larger than L2 at this size)" if ncell * 40 * 2 > 129e6
+                     else "not flushed", "clocks": clk2.stop()}
 
     # per-stage launch times (the dominant stage kernel gives the roofline)
     stage_t = {1: [], 2: [], 3: []}
-    for i in range(max(8, min(args.steps, 64))):
+    for i in range(max(8, min(steps, 64))):
         ensure_room()
         flush.zero_()
         torch.cuda.synchronize()
@@ -545,7 +812,7 @@ def run_ours(args, world, rank, local, dist):
     hv = host.numpy()
     hv[:] = U0
     s.time_setup(case.cfl, 0.0, case.t_end, limit)
-    k_e2e = max(3, min(args.steps, 50 if case.ncells < 4e6 else 10))
+    k_e2e = max(3, min(steps, 50 if case.ncells < 4e6 else 5))
     for _ in range(2):
         s.advance_host(hv, 1)
     hv[:] = U0
@@ -556,8 +823,8 @@ def run_ours(args, world, rank, local, dist):
     e2e_s = time.perf_counter() - t0
     e2e_val = world * ncell * k_e2e / e2e_s
     s.close()
-    return dict(value=value, total=total, clocks=clocks, launches=launches, st_mean=st_mean, dominant=dominant,
-                e2e=e2e_val, ncell=ncell, case=case, tuned=tuned)
+    return dict(value=value, total=total, clocks=clock_rec, launches=launches, st_mean=st_mean, dominant=dominant,
+                e2e=e2e_val, ncell=ncell, case=case, tuned=tuned, durs=durs, sustained=sustained)
 
 
 def main():
@@ -581,6 +848,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: leave out the 3D, sweep, learned and drop-in objects")
     args = ap.parse_args()
     if args.n <= 0:
         args.n = 1024 if args.workload in ("sod2d", "facelist") else 256
@@ -660,7 +929,8 @@ def main():
                 "clocks": r["clocks"], "gpu_launches": r["launches"], "cases_with_status": r["status_bad"]}
         print(json.dumps(line))
         return
-    r = run_ours(args, world, rank, local, dist)
+    default_line = args.workload == "sod2d" and args.order == 1 and not args.no_extras
+    r = run_ours(args, world, rank, local, dist, sustained_s=1.5 if default_line else 0.0)
     if rank != 0:
         return
     hbm_peak, peak_src = read_peaks()
@@ -677,8 +947,9 @@ def main():
         workload = dict(workload, decomposition={"rows_per_chunk" if r["case"].dim == 2 else "planes_per_chunk":
                                                  r["tuned"][0], "warps_per_block": r["tuned"][1] or None,
                                                  "chosen_by": "mmf_autotune"})
-    fp64_peak = 600.9e9   # measured DFMA issue rate on this GB300 (1.91 per SM per clock, operands reused)
-    fp64_peak_mixed = 505.2e9   # measured DADD / DMUL / DFMA with varying operands (1.61 per SM per clock)
+    import minimmerflow_gb300 as mmf
+    # the FP64 issue rate of this GPU, measured in this process (mmf_fp64_rate)
+    fp64_peak, fp64_peak_mixed = mmf.capi.fp64_rate(local)
     line = {
         "metric": metric, "value": r["value"], "unit": metric, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r["total"] / args.steps, "higher_is_better": True,
@@ -698,19 +969,74 @@ def main():
                  "achieved_ops_per_s": fp64_ops * r["value"] / world if fp64_ops else None,
                  "peak_ops_per_s": fp64_peak,
                  "frac": fp64_ops * r["value"] / world / fp64_peak if fp64_ops else None,
-                 "peak_source": "measured DFMA issue rate (probe), not in MEASURED_PEAKS.json",
+                 "peak_source": ("measured in this run: DFMA with reused operands, every SM filled "
+                                 "(mmf_fp64_rate, CUDA events)"),
                  "peak_mixed_ops_per_s": fp64_peak_mixed,
                  "frac_of_mixed": fp64_ops * r["value"] / world / fp64_peak_mixed if fp64_ops else None,
-                 "peak_mixed_source": ("measured rate of DADD, DMUL and DFMA whose operands change from one "
-                                       "instruction to the next (probe)"),
+                 "peak_mixed_source": ("measured in this run: DADD, DMUL and DFMA whose operands change from one "
+                                       "instruction to the next (mmf_fp64_rate, CUDA events)"),
                  "issued_ops_per_cell_update_ncu": ISSUED_FP64_PER_CELL_UPDATE if fp64_ops else None,
+                 "issued_source": "ncu per-opcode counts, profiles/stage2d_fast_sod1024.md",
                  "issued_frac_of_mixed": (ISSUED_FP64_PER_CELL_UPDATE * r["value"] / world / fp64_peak_mixed
                                           if fp64_ops else None)},
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],
+        "step_times": step_stats(r["durs"]),
         "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,
                 "d2h_bytes_per_step": 40 * ncell},
     }
+    if r["sustained"]:
+        line["sustained"] = r["sustained"]
+    if default_line:
+        k_extra, w_extra = max(3, min(args.steps, 10)), max(3, min(args.warmup, 5))
+        # 3D isentropic vortex 256^3, both axes
+        v3 = {}
+        for wl in ("vortex3d_z", "vortex3d_x"):
+            a3 = argparse.Namespace(**vars(args))
+            a3.workload, a3.n, a3.chunk = wl, 256, 0
+            r3 = run_ours(a3, world, rank, local, dist, case=make_case(a3), steps=max(k_extra, 20),
+                          warmup=w_extra, clocks=True)
+            d3 = r3["dominant"]
+            ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
+            v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
+                                    "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),
+                                    "hbm_frac": CELL_BYTES_STEP * r3["value"] / 1e9 / hbm_peak,
+                                    "dominant_stage": {"stage": d3, "achieved_gbs": ach3, "frac": ach3 / hbm_peak},
+                                    "stage_ms": {str(k): 1e3 * v for k, v in r3["st_mean"].items()},
+                                    "planes_per_chunk": r3["tuned"][0], "gpu_launches": r3["launches"],
+                                    "e2e": {"value": r3["e2e"], "unit": metric,
+                                            "h2d_bytes_per_step": 40 * r3["ncell"],
+                                            "d2h_bytes_per_step": 40 * r3["ncell"]},
+                                    "clocks": r3["clocks"]}
+        v3["workload"] = ("3D isentropic vortex 256^3, [-5,5]^3, periodic, beta=5, CFL 0.5, order 1, FP64, "
+                          "fast arithmetic; axis z and axis x")
+        line["vortex3d_256"] = v3
+        # the 512-case sweep at order 2: learned + batched against the plain path
+        sw = run_sweep_comparison(args, local, k_extra, w_extra)
+        sw["workload"] = workload_config(argparse.Namespace(**dict(vars(args), workload="batched", order=2,
+                                                                  learned=True, threshold=sw["threshold"])),
+                                         world)["workload"]
+        line["batched_learned"] = sw
+        # the 3D radial Sod 256^3 with the learned indicator
+        a4 = argparse.Namespace(**vars(args))
+        a4.n, a4.workload = 256, "sod3d_learned"
+        rl = run_learned(a4, world, rank, local, dist, steps=k_extra, warmup=w_extra)
+        o = rl["out"]
+        line["sod3d_learned"] = {
+            "workload": workload_config(a4, world)["workload"],
+            "learned": {"value": o["learned"]["value"], "unit": metric, "ms_per_step": o["learned"]["ms"]},
+            "plain_order2": {"value": o["plain"]["value"], "unit": metric, "ms_per_step": o["plain"]["ms"]},
+            "unlimited_order2": {"value": o["unlimited"]["value"], "unit": metric, "ms_per_step": o["unlimited"]["ms"],
+                                 "meaning": "limiter off on every cell: the most an indicator could save"},
+            "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
+            "ceiling_unlimited_over_plain": o["unlimited"]["value"] / o["plain"]["value"],
+            "limited_fraction_final_state": o["learned"]["limited_fraction"],
+            "vortex3d_l1_error": {"plain": rl["errs"]["plain"], "learned": rl["errs"]["learned"],
+                                  "ratio": rl["errs"]["learned"] / rl["errs"]["plain"],
+                                  "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2" % args.vortex_n},
+            "steps": k_extra}
+        # the minimal drop-in binding (three host round trips per step)
+        line["dropin_binding"] = run_dropin(args, local, max(3, min(args.steps, 5)))
     if not args.no_cpu and args.workload == "sod2d":
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
     print(json.dumps(line))

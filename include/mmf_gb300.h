@@ -342,6 +342,14 @@ int mmf_set_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold);
 int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_cons, double *d_rhs, double *d_max_eig,
                             const int64_t *d_raw_to_cell, void *stream);
 
+/* Measured FP64 instruction rate of a GPU, in thread-level instructions per
+ * second: out[0] for DFMA whose multiplier and addend stay in the same
+ * registers (the pipe's best case), out[1] for DADD, DMUL and DFMA whose
+ * operands change from one instruction to the next (the stage kernels' mix).
+ * The roofline denominator of the FP64-bound stage kernels; no reference
+ * counterpart.  Takes about 0.2 s. */
+int mmf_fp64_rate(int device, double out[2]);
+
 /* Self-test of the reciprocal and square root of MMF_ARITH_FAST (Newton
  * iterations on the hardware approximations): rcp[i] ~ 1/x[i], sqrt[i] ~ sqrt(x[i])
  * for positive x.  No reference counterpart; used to check the error bound. */

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libmmf_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = [("mmf_exact.cu", ["-fmad=false"]), ("mmf_fast.cu", ["-fmad=false"]), ("mmf_capi.cu", []), ("mmf_noalloc.cu", []), ("mmf_batch.cu", []), ("mmf_mlp.cu", []), ("mmf_umesh.cu", ["-fmad=false"]), ("mmf_io.cu", ["-fmad=false"])]
+UNITS = [("mmf_exact.cu", ["-fmad=false"]), ("mmf_fast.cu", ["-fmad=false"]), ("mmf_capi.cu", []), ("mmf_noalloc.cu", []), ("mmf_batch.cu", []), ("mmf_mlp.cu", []), ("mmf_umesh.cu", ["-fmad=false"]), ("mmf_io.cu", ["-fmad=false"]), ("mmf_rate.cu", ["-fmad=false"])]
 
 
 def nvcc():

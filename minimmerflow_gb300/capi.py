@@ -20,7 +20,7 @@ EXPORTS = [
     "mmf_download_state_device", "mmf_compute_rhs", "mmf_compute_polynomials", "mmf_time_setup",
     "mmf_advance", "mmf_advance_async", "mmf_time_info", "mmf_get_stream", "mmf_advance_host", "mmf_last_step_info", "mmf_get_status", "mmf_synchronize",
     "mmf_rk_stage", "mmf_cons2prim", "mmf_prim2cons", "mmf_eval_fluxes", "mmf_eval_splitting",
-    "mmf_eval_bc_values", "mmf_newton_selftest", "mmf_o2_screen_selftest", "mmf_compute_rhs_noalloc", "mmf_set_limiter",
+    "mmf_eval_bc_values", "mmf_fp64_rate", "mmf_newton_selftest", "mmf_o2_screen_selftest", "mmf_compute_rhs_noalloc", "mmf_set_limiter",
     "mmf_set_limiter_flags_device", "mmf_get_limiter_activity",
     "mmf_batch_create", "mmf_batch_destroy", "mmf_batch_cell_count", "mmf_batch_launch_count",
     "mmf_batch_get_stream", "mmf_batch_upload", "mmf_batch_download", "mmf_batch_time_setup",
@@ -107,6 +107,7 @@ def load(build_if_missing=True):
     L.mmf_eval_splitting.argtypes = [C.c_int64, _P, _P, _P, _P, _P]
     L.mmf_eval_bc_values.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P]
     L.mmf_newton_selftest.argtypes = [C.c_int64, _P, _P, _P]
+    L.mmf_fp64_rate.argtypes = [C.c_int, _D]
     L.mmf_o2_screen_selftest.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, _P, _P, _P, _P]
     L.mmf_batch_create.argtypes = [C.c_int, C.POINTER(Grid), C.c_int, C.POINTER(_P)]
     L.mmf_batch_destroy.argtypes = [_P]
@@ -167,6 +168,14 @@ def check(rc):
     if rc != MMF_OK:
         raise MMFError(rc, load().mmf_last_error().decode(errors="replace"))
     return rc
+
+
+def fp64_rate(device=0):
+    """Measured FP64 instruction rate of a GPU (thread-level instructions/s):
+    (DFMA with reused operands, DADD/DMUL/DFMA with varying operands)."""
+    out = (C.c_double * 2)()
+    check(load().mmf_fp64_rate(device, out))
+    return out[0], out[1]
 
 
 def ptr(a):
