@@ -21,10 +21,10 @@ fp64   : the FP64 issue rate measured in this run (mmf_fp64_rate), the bound
 The default line also carries (each with its own workload description):
   vortex3d_256    3D isentropic vortex 256^3, axis z and axis x;
   batched_learned the 512-case order-2 sweep: batched + learned indicator,
-                  batched with every cell limited and with none limited, the
+                  batched with every cell limited and with no cell flagged, the
                   plain per-case path on concurrent streams and one after
                   another, one plain grid of the same size; L1 error ratio;
-  sod3d_learned   3D radial Sod 256^3, order 2, learned / plain / unlimited;
+  sod3d_learned   3D radial Sod 256^3, order 2, learned / plain / no cell flagged;
   dropin_binding  the reference loop through three mmf_compute_rhs host calls
                   per step;
   sustained       about 1.5 s of back-to-back steps with clock samples;
@@ -335,8 +335,9 @@ def run_batched(args, world, rank, local, dist):
 def run_sweep_comparison(args, local, steps, warmup):
     """The 512-case seeded sweep at order 2 (MC limiter), FP64: the batched
     solver with the learned indicator, without it (every cell limited), and
-    with the limiter off everywhere (central slopes: the most any indicator
-    could save, since an indicator only removes limiter work), against the
+    with no cell flagged (central slopes and the positivity fallback
+    everywhere: the most any indicator could save, since an indicator only
+    removes limiter work), against the
     same cases run by the plain per-case path -- one context per case, all
     contexts' steps enqueued on their own streams at once so that the GPU
     overlaps them (a fair plain alternative), and one after another (the
@@ -366,10 +367,13 @@ def run_sweep_comparison(args, local, steps, warmup):
     packed = b.pack(states)
     stream = torch.cuda.ExternalStream(b.stream_handle, device=torch.device("cuda", local))
     finals = {}
-    for mode in ("learned", "limited", "unlimited"):
+    # "no_cell_flagged": the flagged mode with the flags as created (all zero),
+    # central slopes and the positivity fallback on every cell -- what the
+    # learned path would cost with an indicator that is free and flags nothing
+    for mode in ("no_cell_flagged", "limited", "learned"):
         b.set_indicator(mlp if mode == "learned" else None, thr)
-        if mode == "unlimited":
-            b.set_limiter("none")
+        if mode == "no_cell_flagged":
+            b.set_limiter("flagged")
         b.upload(packed)
         b.time_setup(max_steps=10 ** 9)
         chunk, bps = b.autotune(trial_steps=2)
@@ -389,7 +393,7 @@ def run_sweep_comparison(args, local, steps, warmup):
             durs.append(e0.elapsed_time(e1) / 1e3)
         out[mode] = {"value": total * steps / sum(durs), "unit": "cell-updates/s", "step_times": step_stats(durs),
                      "launches": b.launch_count - l0, "chunk": chunk, "blocks_per_sm": bps}
-        if mode != "unlimited":
+        if mode != "no_cell_flagged":
             finals[mode] = (b.run(states, 20), [b.case_info(i)[0] for i in range(len(cases))])
     b.close()
     del packed
@@ -471,7 +475,7 @@ def run_sweep_comparison(args, local, steps, warmup):
                                        "sweep's total cells" % (n1, n1)}
     out["learned_over_plain_concurrent"] = out["learned"]["value"] / out["plain_concurrent_streams"]["value"]
     out["learned_over_batched_limited"] = out["learned"]["value"] / out["limited"]["value"]
-    out["ceiling_unlimited_over_limited"] = out["unlimited"]["value"] / out["limited"]["value"]
+    out["ceiling_no_cell_flagged_over_limited"] = out["no_cell_flagged"]["value"] / out["limited"]["value"]
     return out
 
 
@@ -532,8 +536,8 @@ def run_dropin(args, local, steps):
 
 def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
     """3D radial Sod (order 2, MC limiter) with and without the learned
-    troubled-cell indicator, and with the limiter off everywhere (the most an
-    indicator could save); accuracy against the exact solution on a 3D
+    troubled-cell indicator, and with no cell flagged (central slopes and the
+    positivity fallback everywhere: the most an indicator could save); accuracy against the exact solution on a 3D
     isentropic vortex with the first two settings."""
     steps = args.steps if steps is None else steps
     warmup = args.warmup if warmup is None else warmup
@@ -554,12 +558,12 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
     U0 = case.initial_state()
     out = {}
     finals = {}
-    for mode in ("plain", "learned", "unlimited"):
+    for mode in ("plain", "learned", "no_cell_flagged"):
         s = case.solver(arith=args.arith, device=local, order=2)
         if mode == "learned":
             indicator.use_indicator(s, mlp, args.threshold)
-        if mode == "unlimited":
-            s.set_limiter("none")
+        if mode == "no_cell_flagged":
+            s.set_limiter("flagged", flags=np.zeros(case.ncells, dtype=np.uint8))
         stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
         s.upload(U0)
         s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
@@ -582,7 +586,7 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
         value, total = replica_throughput(sum(durs), case.ncells * steps, world, dist)
         out[mode] = dict(value=value, ms=1e3 * total / steps,
                          launches=s.launch_count - launches0, status=s.status(), step_times=step_stats(durs))
-        if mode != "unlimited":
+        if mode != "no_cell_flagged":
             finals[mode] = s.download()
         if mode == "learned":
             _, flags = indicator.run_indicator(s, mlp, args.threshold)
@@ -989,54 +993,76 @@ def main():
         line["sustained"] = r["sustained"]
     if default_line:
         k_extra, w_extra = max(3, min(args.steps, 10)), max(3, min(args.warmup, 5))
-        # 3D isentropic vortex 256^3, both axes
-        v3 = {}
-        for wl in ("vortex3d_z", "vortex3d_x"):
-            a3 = argparse.Namespace(**vars(args))
-            a3.workload, a3.n, a3.chunk = wl, 256, 0
-            r3 = run_ours(a3, world, rank, local, dist, case=make_case(a3), steps=max(k_extra, 20),
-                          warmup=w_extra, clocks=True)
-            d3 = r3["dominant"]
-            ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
-            v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
-                                    "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),
-                                    "hbm_frac": CELL_BYTES_STEP * r3["value"] / 1e9 / hbm_peak,
-                                    "dominant_stage": {"stage": d3, "achieved_gbs": ach3, "frac": ach3 / hbm_peak},
-                                    "stage_ms": {str(k): 1e3 * v for k, v in r3["st_mean"].items()},
-                                    "planes_per_chunk": r3["tuned"][0], "gpu_launches": r3["launches"],
-                                    "e2e": {"value": r3["e2e"], "unit": metric,
-                                            "h2d_bytes_per_step": 40 * r3["ncell"],
-                                            "d2h_bytes_per_step": 40 * r3["ncell"]},
-                                    "clocks": r3["clocks"]}
-        v3["workload"] = ("3D isentropic vortex 256^3, [-5,5]^3, periodic, beta=5, CFL 0.5, order 1, FP64, "
-                          "fast arithmetic; axis z and axis x")
-        line["vortex3d_256"] = v3
-        # the 512-case sweep at order 2: learned + batched against the plain path
-        sw = run_sweep_comparison(args, local, k_extra, w_extra)
-        sw["workload"] = workload_config(argparse.Namespace(**dict(vars(args), workload="batched", order=2,
-                                                                  learned=True, threshold=sw["threshold"])),
-                                         world)["workload"]
-        line["batched_learned"] = sw
-        # the 3D radial Sod 256^3 with the learned indicator
-        a4 = argparse.Namespace(**vars(args))
-        a4.n, a4.workload = 256, "sod3d_learned"
-        rl = run_learned(a4, world, rank, local, dist, steps=k_extra, warmup=w_extra)
-        o = rl["out"]
-        line["sod3d_learned"] = {
-            "workload": workload_config(a4, world)["workload"],
-            "learned": {"value": o["learned"]["value"], "unit": metric, "ms_per_step": o["learned"]["ms"]},
-            "plain_order2": {"value": o["plain"]["value"], "unit": metric, "ms_per_step": o["plain"]["ms"]},
-            "unlimited_order2": {"value": o["unlimited"]["value"], "unit": metric, "ms_per_step": o["unlimited"]["ms"],
-                                 "meaning": "limiter off on every cell: the most an indicator could save"},
-            "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
-            "ceiling_unlimited_over_plain": o["unlimited"]["value"] / o["plain"]["value"],
-            "limited_fraction_final_state": o["learned"]["limited_fraction"],
-            "vortex3d_l1_error": {"plain": rl["errs"]["plain"], "learned": rl["errs"]["learned"],
-                                  "ratio": rl["errs"]["learned"] / rl["errs"]["plain"],
-                                  "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2" % args.vortex_n},
-            "steps": k_extra}
-        # the minimal drop-in binding (three host round trips per step)
-        line["dropin_binding"] = run_dropin(args, local, max(3, min(args.steps, 5)))
+
+        def guarded(key, fn):
+            """An extra object of the line; a failure is recorded in it and
+            does not cost the line."""
+            t0 = time.time()
+            try:
+                line[key] = fn()
+            except Exception as exc:   # noqa: BLE001 -- reported in the line
+                line[key] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+            print("[bench] %s: %.1f s" % (key, time.time() - t0), file=sys.stderr, flush=True)
+
+        def vortex3d():
+            v3 = {}
+            for wl in ("vortex3d_z", "vortex3d_x"):
+                a3 = argparse.Namespace(**vars(args))
+                a3.workload, a3.n, a3.chunk = wl, 256, 0
+                r3 = run_ours(a3, world, rank, local, dist, case=make_case(a3), steps=max(k_extra, 20),
+                              warmup=w_extra, clocks=True)
+                d3 = r3["dominant"]
+                ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
+                v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
+                                        "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),
+                                        "hbm_frac": CELL_BYTES_STEP * r3["value"] / 1e9 / hbm_peak,
+                                        "dominant_stage": {"stage": d3, "achieved_gbs": ach3,
+                                                           "frac": ach3 / hbm_peak},
+                                        "stage_ms": {str(k): 1e3 * v for k, v in r3["st_mean"].items()},
+                                        "planes_per_chunk": r3["tuned"][0],
+                                        "kernel": "tile" if r3["tuned"][1] == -1 else "row blocks",
+                                        "gpu_launches": r3["launches"],
+                                        "e2e": {"value": r3["e2e"], "unit": metric,
+                                                "h2d_bytes_per_step": 40 * r3["ncell"],
+                                                "d2h_bytes_per_step": 40 * r3["ncell"]},
+                                        "clocks": r3["clocks"]}
+            v3["workload"] = ("3D isentropic vortex 256^3, [-5,5]^3, periodic, beta=5, CFL 0.5, order 1, FP64, "
+                              "fast arithmetic; axis z and axis x")
+            return v3
+
+        def sweep():
+            sw = run_sweep_comparison(args, local, k_extra, w_extra)
+            sw["workload"] = workload_config(argparse.Namespace(**dict(vars(args), workload="batched", order=2,
+                                                                      learned=True, threshold=sw["threshold"])),
+                                             world)["workload"]
+            return sw
+
+        def learned3d():
+            a4 = argparse.Namespace(**vars(args))
+            a4.n, a4.workload = 256, "sod3d_learned"
+            rl = run_learned(a4, world, rank, local, dist, steps=k_extra, warmup=w_extra)
+            o = rl["out"]
+            return {
+                "workload": workload_config(a4, world)["workload"],
+                "learned": {"value": o["learned"]["value"], "unit": metric, "ms_per_step": o["learned"]["ms"]},
+                "plain_order2": {"value": o["plain"]["value"], "unit": metric, "ms_per_step": o["plain"]["ms"]},
+                "no_cell_flagged": {"value": o["no_cell_flagged"]["value"], "unit": metric,
+                                    "ms_per_step": o["no_cell_flagged"]["ms"],
+                                    "meaning": "central slopes and the positivity fallback on every cell, no "
+                                               "indicator run: the most an indicator could save"},
+                "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
+                "ceiling_no_cell_flagged_over_plain": o["no_cell_flagged"]["value"] / o["plain"]["value"],
+                "limited_fraction_final_state": o["learned"]["limited_fraction"],
+                "vortex3d_l1_error": {"plain": rl["errs"]["plain"], "learned": rl["errs"]["learned"],
+                                      "ratio": rl["errs"]["learned"] / rl["errs"]["plain"],
+                                      "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2"
+                                              % args.vortex_n},
+                "steps": k_extra}
+
+        guarded("vortex3d_256", vortex3d)
+        guarded("batched_learned", sweep)
+        guarded("sod3d_learned", learned3d)
+        guarded("dropin_binding", lambda: run_dropin(args, local, max(3, min(args.steps, 5))))
     if not args.no_cpu and args.workload == "sod2d":
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
     print(json.dumps(line))

@@ -31,7 +31,7 @@ EXPORTS = [
     "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
     "mmf_umesh_create", "mmf_umesh_destroy", "mmf_umesh_launch_count", "mmf_umesh_upload", "mmf_umesh_download",
     "mmf_umesh_compute_rhs", "mmf_umesh_time_setup", "mmf_umesh_advance",
-    "mmf_autotune", "mmf_set_step_log", "mmf_get_step_log", "mmf_init_state", "mmf_l1_density_error", "mmf_write_vtk", "mmf_save_checkpoint", "mmf_load_checkpoint",
+    "mmf_autotune", "mmf_set_shape", "mmf_set_step_log", "mmf_get_step_log", "mmf_init_state", "mmf_l1_density_error", "mmf_write_vtk", "mmf_save_checkpoint", "mmf_load_checkpoint",
 ]
 LIMIT_ALL, LIMIT_NONE, LIMIT_FLAGGED = 0, 1, 2
 NOALLOC_MAX_CELLS = 65536
@@ -152,6 +152,7 @@ def load(build_if_missing=True):
     L.mmf_umesh_time_setup.argtypes = [_P, C.c_double, C.c_double, C.c_double, C.c_int64]
     L.mmf_umesh_advance.argtypes = [_P, C.c_int64, _D, C.POINTER(C.c_int64)]
     L.mmf_autotune.argtypes = [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mmf_set_shape.argtypes = [_P, C.c_int, C.c_int]
     L.mmf_set_step_log.argtypes = [_P, C.c_int64]
     L.mmf_get_step_log.argtypes = [_P, _P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.mmf_init_state.argtypes = [_P, C.POINTER(Problem)]

@@ -177,7 +177,7 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;
     gp.half_area_per_vol = 0.5 * gp.area / gp.vol;
-    plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D);
+    plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D, 0, grid->order == 1 ? TILE3D_DEFAULT : 0);
     const size_t bytes = sizeof(double) * NF * (size_t)gp.plane;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->U, bytes);
@@ -1086,17 +1086,22 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
         for (int ch : {8, 12, 16, 20, 24, 28, 30, 32, 40, 48, 64})
             for (int w : {1, 2, 4}) cand.emplace_back(ch, w);
     } else {
-        for (int ch : {4, 6, 8, 12, 14, 16, 24, 32, 64}) cand.emplace_back(ch, 0);
+        // order 1: both 3D kernels (second = 1: tile kernel); order 2: row blocks
+        for (int ch : {4, 6, 8, 12, 14, 16, 24, 32, 64}) {
+            cand.emplace_back(ch, 0);
+            if (c->grid.order == 1) cand.emplace_back(ch, 1);
+        }
     }
     const int by = c->grid.order == 2 ? BY3D_O2 : BY3D;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     MMF_CUDA(cudaEventCreate(&e0));
     MMF_CUDA(cudaEventCreate(&e1));
-    std::pair<int, int> best(c->gp.chunk, c->gp.wpb);
     float best_ms = 1e30f;
     cudaError_t e = cudaSuccess;
+    const bool d2 = c->gp.dim == 2;
+    std::pair<int, int> best(c->gp.chunk, d2 ? c->gp.wpb : c->gp.tile3d);
     for (const auto &cd : cand) {
-        plan_cartesian(c->gp, cd.first, by, cd.second);
+        plan_cartesian(c->gp, cd.first, by, d2 ? cd.second : 0, d2 ? 0 : cd.second);
         e = cudaMemcpyAsync(c->U, c->aos, bytes, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->ctrl, &trial, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = c->rk_step();
@@ -1111,7 +1116,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    plan_cartesian(c->gp, best.first, by, best.second);
+    plan_cartesian(c->gp, best.first, by, d2 ? best.second : 0, d2 ? 0 : best.second);
     if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
     if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
     MMF_CUDA(e);
@@ -1119,7 +1124,23 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     MMF_CUDA(cudaMemcpyAsync(c->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     if (chunk_out) *chunk_out = c->gp.chunk;
-    if (warps_out) *warps_out = c->gp.dim == 2 ? c->gp.wpb : 0;
+    if (warps_out) *warps_out = d2 ? c->gp.wpb : (c->gp.tile3d ? -1 : 0);
+    return MMF_OK;
+}
+
+int mmf_set_shape(mmf_ctx *c, int chunk, int variant)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (chunk < 1) return fail(MMF_ERR_ARG, "chunk must be >= 1");
+    const bool d2 = c->gp.dim == 2;
+    if (d2 && (variant < 1 || variant > WARPS_2D)) return fail(MMF_ERR_ARG, "2D: warps per block must be 1..4");
+    if (!d2 && variant != 0 && variant != 1) return fail(MMF_ERR_ARG, "3D: variant must be 0 (row blocks) or 1 (tiles)");
+    if (!d2 && variant == 1 && c->grid.order != 1) return fail(MMF_ERR_UNSUPPORTED, "the 3D tile kernel is order 1");
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
+    plan_cartesian(c->gp, chunk, c->grid.order == 2 ? BY3D_O2 : BY3D, d2 ? variant : 0, d2 ? 0 : variant);
+    if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+    if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
     return MMF_OK;
 }
 

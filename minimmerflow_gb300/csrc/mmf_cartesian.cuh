@@ -59,6 +59,7 @@ struct GridParams {
     int chunk0;     // first chunk of the launch (a launch may cover a band of the grid)
     int bookkeep;   // this launch updates the control block (exactly one launch per stage)
     int wpb;        // 2D: warps per block
+    int tile3d;     // 3D order 1: 1 = 32 x 16 tile kernel, 0 = row-block kernel
     long long plane;  // cells per field plane
 };
 
@@ -510,6 +511,179 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
             if (lane == 0 && status) atomicOr(&sa.ctrl->status, status);
         }
     }
+}
+
+// ---------------------------------------------------------- 3D tile kernel
+// Block = 16 warps over a tile of 32 x 16 cells (x = lane, y = warp) that
+// marches along z.  Every lane and warp owns an output cell, so tiles divide
+// 256-cell grid lines exactly.  The records the tile's faces need from the
+// four neighbouring lines (the column left and right of the tile, the row
+// below and above it) are evaluated once per plane by three warps in one
+// extra pass each (x or y part only), and the faces on the tile's left and
+// bottom edges by two more warps; every other face is evaluated once, by the
+// cell on its low side: x faces move between lanes by shuffles, y faces go
+// through shared memory, z faces stay in registers along the march.
+// Barriers per plane: records published, faces published, shared memory free.
+constexpr int TILE_X = 32, TILE_Y = 16;
+constexpr int TW_TOP = 4, TW_BOT = 9, TW_SIDE = 14;   // warps of the halo-record passes
+constexpr int TW_LEFTF = 3, TW_BOTF = 15;             // warps of the edge-face passes
+
+template <int NV>
+struct SmemTile {
+    double yc[TILE_Y + 1][NV][32];   // y-face side (state, y flux, y speed) of rows 0..15 and the top halo row
+    double yf[TILE_Y + 1][NV][32];
+    double ylam[TILE_Y + 1][32];
+    double bc[NV][32], bf[NV][32], blam[32];                        // bottom halo row
+    double xc[2][NV][TILE_Y], xf[2][NV][TILE_Y], xlam[2][TILE_Y];    // left [0] / right [1] halo column
+    double c0[NV][TILE_Y], f0[NV][TILE_Y], lam0[TILE_Y];            // column 0 of the tile (x side)
+    double Fy[TILE_Y][NV][32];       // y face above row w
+    double Fl[NV][TILE_Y];           // x face on the tile's left edge, row w
+    double Fb[NV][32];               // y face on the tile's bottom edge, column l
+};
+
+template <class A, int STAGE>
+__global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParams gp, StageArgs sa)
+{
+    constexpr int NV = A::NVAR;
+    __shared__ SmemTile<NV> sm;
+    const int l = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const StepScalars sc = step_scalars<A, STAGE>(gp, sa.ctrl);
+    if (gp.bookkeep && blockIdx.x == 0 && threadIdx.x == 0) step_bookkeeping<STAGE>(sa.ctrl, sc);
+    if (!sc.active) return;
+
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    const int ntx = (nx + TILE_X - 1) / TILE_X, nty = (ny + TILE_Y - 1) / TILE_Y;
+    int b = blockIdx.x;
+    const int tx = b % ntx; b /= ntx;
+    const int ty = b % nty; b /= nty;
+    const int chunk = gp.chunk0 + b;
+    const int x0 = tx * TILE_X, y0 = ty * TILE_Y;
+    const int x = x0 + l, y = y0 + w;
+    const int z0 = chunk * gp.chunk;
+    const int z1 = min(z0 + gp.chunk, nz);
+    const bool out = (x < nx) && (y < ny);
+    const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
+               perz = gp.bc_lo[2] == BC_PERIODIC;
+    unsigned status = 0;
+    unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
+    double lmax = 0.0;
+
+    RecOf<A, 3> cur, nxt;
+    double Fzlo[NV], Fzhi[NV], Fxl[NV], Fxr[NV], Fyb[NV], Fyt[NV], acc[NV];
+    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, nxt, nullptr);
+    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
+    {
+        const double lz = face_dir<A, 3>(nxt, cur, 2, Fzlo);
+        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+    }
+    for (int z = z0; z < z1; ++z) {
+        // halo records of plane z (the part of the record their faces use)
+        if (w == TW_TOP || w == TW_BOT) {
+            RecOf<A, 3> h;
+            load_record<A, STAGE, 3>(sa, gp, sc, x, w == TW_TOP ? y0 + TILE_Y : y0 - 1, z, h, nullptr);
+            if (w == TW_TOP) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { sm.yc[TILE_Y][k][l] = h.c[k]; sm.yf[TILE_Y][k][l] = h.f[1][k]; }
+                sm.ylam[TILE_Y][l] = h.lam[1];
+            } else {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { sm.bc[k][l] = h.c[k]; sm.bf[k][l] = h.f[1][k]; }
+                sm.blam[l] = h.lam[1];
+            }
+        } else if (w == TW_SIDE) {
+            const int side = l >> 4, r = l & 15;
+            RecOf<A, 3> h;
+            load_record<A, STAGE, 3>(sa, gp, sc, side ? x0 + TILE_X : x0 - 1, y0 + r, z, h, nullptr);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.xc[side][k][r] = h.c[k]; sm.xf[side][k][r] = h.f[0][k]; }
+            sm.xlam[side][r] = h.lam[0];
+        }
+        // this row's y side, and column 0's x side
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.yc[w][k][l] = cur.c[k]; sm.yf[w][k][l] = cur.f[1][k]; }
+        sm.ylam[w][l] = cur.lam[1];
+        if (l == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.c0[k][w] = cur.c[k]; sm.f0[k][w] = cur.f[0][k]; }
+            sm.lam0[w] = cur.lam[0];
+        }
+        __syncthreads();
+        // x face on the right: the next lane, or the right halo column
+        {
+            double cR[NV], fR[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { cR[k] = shfl_down(cur.c[k], 1); fR[k] = shfl_down(cur.f[0][k], 1); }
+            double lamR = shfl_down(cur.lam[0], 1);
+            if (l == 31) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { cR[k] = sm.xc[1][k][w]; fR[k] = sm.xf[1][k][w]; }
+                lamR = sm.xlam[1][w];
+            }
+            const double lx = A::face(cur.c, cur.f[0], cur.lam[0], cR, fR, lamR, Fxr);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lx);
+        }
+        // y face above: the next row, or the top halo row
+        {
+            double cU[NV], fU[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { cU[k] = sm.yc[w + 1][k][l]; fU[k] = sm.yf[w + 1][k][l]; }
+            const double ly = A::face(cur.c, cur.f[1], cur.lam[1], cU, fU, sm.ylam[w + 1][l], Fyt);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sm.Fy[w][k][l] = Fyt[k];
+        }
+        // faces on the tile's left edge (lanes 0..15: rows) and bottom edge (lanes: columns)
+        if (w == TW_LEFTF) {
+            const int r = l & 15;
+            double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                cL[k] = sm.xc[0][k][r]; fL[k] = sm.xf[0][k][r]; cR[k] = sm.c0[k][r]; fR[k] = sm.f0[k][r];
+            }
+            const double le = A::face(cL, fL, sm.xlam[0][r], cR, fR, sm.lam0[r], F);
+            if (l < 16) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.Fl[k][r] = F[k];
+                if (STAGE <= STAGE_1 && x0 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
+            }
+        } else if (w == TW_BOTF) {
+            double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                cL[k] = sm.bc[k][l]; fL[k] = sm.bf[k][l]; cR[k] = sm.yc[0][k][l]; fR[k] = sm.yf[0][k][l];
+            }
+            const double le = A::face(cL, fL, sm.blam[l], cR, fR, sm.ylam[0][l], F);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sm.Fb[k][l] = F[k];
+            if (STAGE <= STAGE_1 && x < nx && y0 < ny) lmax = max_nonneg(lmax, le);
+        }
+        __syncthreads();
+        // the faces below and on the left: the previous lane / row, or the tile edge
+        const int wb = (w > 0) ? w - 1 : 0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double fl = shfl_up(Fxr[k], 1);
+            Fxl[k] = (l == 0) ? sm.Fl[k][w] : fl;
+            Fyb[k] = (w == 0) ? sm.Fb[k][l] : sm.Fy[wb][k][l];
+        }
+        accumulate_pair<A, true>(acc, Fxl, Fxr, gp.area, perx && x == nx - 1);
+        accumulate_pair<A, false>(acc, Fyb, Fyt, gp.area, pery && y == ny - 1);
+        // plane z+1 and the z face
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, nxt, (z + 1 < z1) ? st : nullptr);
+        const double lz = face_dir<A, 3>(cur, nxt, 2, Fzhi);
+        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+        if (out) {
+            accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
+            store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
+                                   acc, cur.c);
+        }
+        __syncthreads();
+        cur = nxt;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
+    }
+    publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }
 
 } // namespace mmf

@@ -15,13 +15,16 @@ namespace mmf {
 constexpr int BY3D = 16;        // warps per 3D block (14 output rows + 2 halo rows)
 constexpr int WARPS_2D = 4;     // warps per 2D block
 constexpr int BY3D_O2 = 8;      // warps per 3D order-2 block (face-side records need twice the registers)
+constexpr int TILE3D_DEFAULT = 1;   // order-1 3D kernel when nothing else is chosen: the tile kernel
 
 // Fills the decomposition fields of gp for the given marching chunk; 'by' is
-// the number of warps a 3D block stacks in y (two of them halo rows).
-inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0)
+// the number of warps a 3D block stacks in y (two of them halo rows) in the
+// row-block kernel; tile3d selects the 3D tile kernel (order 1 only).
+inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0, int tile3d = 0)
 {
     gp.nseg = (gp.n[0] + SEG - 1) / SEG;
     gp.wpb = (wpb >= 1 && wpb <= WARPS_2D) ? wpb : WARPS_2D;
+    gp.tile3d = (gp.dim == 3 && tile3d) ? 1 : 0;
     gp.chunk0 = 0;
     gp.bookkeep = 1;
     if (gp.dim == 2) {
@@ -43,6 +46,8 @@ inline long long cartesian_blocks(const GridParams &gp)
         long long warps = (long long)gp.nseg * gp.nchunk;
         return (warps + gp.wpb - 1) / gp.wpb;
     }
+    if (gp.tile3d)
+        return (long long)((gp.n[0] + TILE_X - 1) / TILE_X) * ((gp.n[1] + TILE_Y - 1) / TILE_Y) * gp.nchunk;
     return (long long)gp.nseg * gp.nrowblk * gp.nchunk;
 }
 
@@ -53,8 +58,12 @@ inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cud
     if (gp.dim == 2) {
         stage2d_kernel<A, STAGE><<<blocks, gp.wpb * 32, 0, s>>>(gp, sa);
     } else {
-        if constexpr (HAS3D) stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
-        else return cudaErrorInvalidValue;
+        if constexpr (HAS3D) {
+            if (gp.tile3d) stage3d_tile_kernel<A, STAGE><<<blocks, TILE_X * TILE_Y, 0, s>>>(gp, sa);
+            else stage3d_kernel<A, STAGE, BY3D><<<blocks, BY3D * 32, 0, s>>>(gp, sa);
+        } else {
+            return cudaErrorInvalidValue;
+        }
     }
     return cudaPeekAtLastError();
 }

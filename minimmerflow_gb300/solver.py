@@ -194,6 +194,11 @@ class CartesianEuler:
     def launch_count(self):
         return self._lib.mmf_launch_count(self._ctx)
 
+    def set_shape(self, chunk, variant):
+        """Pin the decomposition: rows / planes per chunk, and warps per block
+        (2D) or the 3D kernel (0 = row blocks, 1 = tiles)."""
+        capi.check(self._lib.mmf_set_shape(self._ctx, chunk, variant))
+
     def autotune(self, trial_steps=4):
         """Pick the stage kernels' decomposition by timing (state restored);
         returns (chunk, warps_per_block)."""

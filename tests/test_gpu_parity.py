@@ -141,6 +141,36 @@ def test_compute_rhs_ragged_bitwise(orc, mmf, dim, n, periodic):
     assert np.array_equal(R, R_ref)
 
 
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+@pytest.mark.parametrize("n,periodic", [((61, 14, 9), False), ((40, 35, 11), True), ((32, 16, 8), True),
+                                        ((1, 17, 5), False)])
+def test_3d_kernels_give_the_same_bits(orc, mmf, arith, n, periodic):
+    """The two 3D order-1 kernels -- row blocks of 30-column segments with
+    halo lanes and rows, and 32 x 16 tiles with one-pass halo records -- and
+    every plane chunk give the same bits, on grids that the tiles divide and
+    on ragged ones; with the reference arithmetic they are the oracle's."""
+    P = mmf.problem
+    case = P.Case("ragged3d", P.RADSOD, 3, n, (-0.3, -0.2, -0.1), 1.0, 0.5, periodic=periodic,
+                  prm=P.Params(sod_radius=0.3))
+    m = oracle_mesh(orc, case)
+    rng = np.random.default_rng(5)
+    U0 = m.initial_state(oracle_params(orc, case)) * (1.0 + 0.05 * rng.standard_normal((m.ncells, 1)))
+    steps = 6
+    outs = []
+    for variant, chunk in [(0, 4), (1, 4), (1, 3), (1, 64)]:
+        with case.solver(arith=arith) as s:
+            s.set_shape(chunk, variant)
+            U, t, done = s.run(U0, case.cfl, max_steps=steps)
+            assert done == steps and s.status() == 0
+        outs.append((U, t))
+    for U, t in outs[1:]:
+        assert t == outs[0][1]
+        assert np.array_equal(U, outs[0][0])
+    if arith == "reference":
+        U_ref, t_ref, _ = m.run(U0, case.cfl, max_steps=steps)
+        assert outs[0][1] == t_ref and np.array_equal(outs[0][0], U_ref)
+
+
 def test_compute_rhs_morton_map(orc, mmf):
     """Raw ids in octree (Morton) order, as bitpit stores VolOctree cells."""
     case = mmf.problem.reference_case("radsod", 3, 16)
