@@ -27,7 +27,7 @@ EXPORTS = [
     "mmf_batch_advance_async", "mmf_batch_synchronize", "mmf_batch_case_info", "mmf_batch_set_shape",
     "mmf_batch_get_shape", "mmf_batch_autotune", "mmf_batch_set_limiter", "mmf_batch_set_indicator",
     "mmf_mlp_create", "mmf_mlp_destroy", "mmf_mlp_num_params", "mmf_mlp_input_width", "mmf_mlp_get_params",
-    "mmf_mlp_set_params", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
+    "mmf_mlp_set_params", "mmf_mlp_set_wait_limits", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
     "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
     "mmf_umesh_create", "mmf_umesh_destroy", "mmf_umesh_launch_count", "mmf_umesh_upload", "mmf_umesh_download",
     "mmf_umesh_compute_rhs", "mmf_umesh_time_setup", "mmf_umesh_advance",
@@ -138,6 +138,7 @@ def load(build_if_missing=True):
     L.mmf_mlp_gradients.argtypes = [_P, _P, _P, C.c_int64, _P, C.POINTER(C.c_float)]
     L.mmf_mlp_train_batch.argtypes = [_P, _P, _P, C.c_int64, C.c_float, C.POINTER(C.c_float)]
     L.mmf_mlp_predict.argtypes = [_P, _P, C.c_int64, _P]
+    L.mmf_mlp_set_wait_limits.argtypes = [_P, C.c_int64, C.c_int64]
     L.mmf_features.argtypes = [_P, _P]
     L.mmf_indicator.argtypes = [_P, _P, C.c_float, _P, _P]
     L.mmf_set_indicator.argtypes = [_P, _P, C.c_float]

@@ -31,18 +31,19 @@ struct mmf_mlp {
     int device = 0;
     cudaStream_t stream = nullptr;
     float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
-    __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w2t = nullptr, *w1c = nullptr, *w2c = nullptr;
+    __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w2t = nullptr, *w1c = nullptr, *w2c = nullptr, *w2tc = nullptr;
     int *err = nullptr;
     long long adam_t = 0;
     long long n = 0;
+    WaitLimits lim{1ll << 22, 0};   // inference kernel: mbarrier wait limit, probe wait (0 = none)
 };
 
 namespace mmf {
 
 static int mlp_pack(mmf_mlp *p)
 {
-    if (p->dim == 3) mlp_pack_kernel<3><<<64, 256, 0, p->stream>>>(p->params, p->w1, p->w2, p->w2t, p->w1c, p->w2c);
-    else mlp_pack_kernel<2><<<64, 256, 0, p->stream>>>(p->params, p->w1, p->w2, p->w2t, p->w1c, p->w2c);
+    if (p->dim == 3) mlp_pack_kernel<3><<<64, 256, 0, p->stream>>>(p->params, p->w1, p->w2, p->w2t, p->w1c, p->w2c, p->w2tc);
+    else mlp_pack_kernel<2><<<64, 256, 0, p->stream>>>(p->params, p->w1, p->w2, p->w2t, p->w1c, p->w2c, p->w2tc);
     MLP_CUDA(cudaPeekAtLastError());
     return MMF_OK;
 }
@@ -63,7 +64,7 @@ static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const double *
     w.w1c = p->w1c;
     w.w2c = p->w2c;
     w.params = p->params;
-    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, U, X, w, thr, prob, flags, p->err, bg);
+    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, U, X, w, thr, prob, flags, p->err, bg, p->lim);
     return cudaPeekAtLastError();
 }
 
@@ -133,6 +134,7 @@ int mmf_mlp_create(int dim, uint64_t seed, int device, mmf_mlp **out)
     if (e == cudaSuccess) e = cudaMalloc(&p->w2, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
     if (e == cudaSuccess) e = cudaMalloc(&p->w2t, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
     if (e == cudaSuccess) e = cudaMalloc(&p->w2c, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
+    if (e == cudaSuccess) e = cudaMalloc(&p->w2tc, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
     if (e == cudaSuccess) e = cudaMemset(p->m, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(p->v, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
@@ -162,7 +164,7 @@ int mmf_mlp_destroy(mmf_mlp *p)
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
     cudaFree(p->params); cudaFree(p->grad); cudaFree(p->m); cudaFree(p->v); cudaFree(p->loss); cudaFree(p->err);
-    cudaFree(p->w1); cudaFree(p->w1c); cudaFree(p->w2); cudaFree(p->w2t); cudaFree(p->w2c);
+    cudaFree(p->w1); cudaFree(p->w1c); cudaFree(p->w2); cudaFree(p->w2t); cudaFree(p->w2c); cudaFree(p->w2tc);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return MMF_OK;
@@ -196,13 +198,24 @@ static int run_train(mmf_mlp *p, const void *d_X, const unsigned char *d_y, int6
     if (B < 16 || B % 16) return set_last_error(MMF_ERR_ARG, "batch must be a positive multiple of 16");
     MLP_CUDA(cudaMemsetAsync(p->grad, 0, sizeof(float) * (size_t)p->n, p->stream));
     MLP_CUDA(cudaMemsetAsync(p->loss, 0, sizeof(float), p->stream));
-    const unsigned blocks = (unsigned)((B / 16 + TRAIN_WARPS - 1) / TRAIN_WARPS);
-    if (p->dim == 3)
-        mlp_train_kernel<3><<<blocks, TRAIN_WARPS * 32, 0, p->stream>>>((const __nv_bfloat16 *)d_X, d_y, (int)B, p->w1,
-                                                                         p->w2, p->w2t, p->params, p->grad, p->loss);
-    else
-        mlp_train_kernel<2><<<blocks, TRAIN_WARPS * 32, 0, p->stream>>>((const __nv_bfloat16 *)d_X, d_y, (int)B, p->w1,
-                                                                         p->w2, p->w2t, p->params, p->grad, p->loss);
+    MLP_CUDA(cudaMemsetAsync(p->err, 0, sizeof(int), p->stream));
+    const unsigned blocks = (unsigned)((B + 127) / 128);
+    MlpTrainDev w;
+    w.w1c = p->w1c;
+    w.w2c = p->w2c;
+    w.w2tc = p->w2tc;
+    w.params = p->params;
+    if (p->dim == 3) {
+        MLP_CUDA(cudaFuncSetAttribute(mlp_train_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      mlp_train_tc_smem<3>()));
+        mlp_train_tc_kernel<3><<<blocks, 128, mlp_train_tc_smem<3>(), p->stream>>>(
+            (const __nv_bfloat16 *)d_X, d_y, (int)B, w, p->grad, p->loss, p->err, p->lim);
+    } else {
+        MLP_CUDA(cudaFuncSetAttribute(mlp_train_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      mlp_train_tc_smem<2>()));
+        mlp_train_tc_kernel<2><<<blocks, 128, mlp_train_tc_smem<2>(), p->stream>>>(
+            (const __nv_bfloat16 *)d_X, d_y, (int)B, w, p->grad, p->loss, p->err, p->lim);
+    }
     MLP_CUDA(cudaPeekAtLastError());
     return MMF_OK;
 }
@@ -218,6 +231,7 @@ int mmf_mlp_gradients(mmf_mlp *p, const void *d_X, const unsigned char *d_y, int
     if (grad_out) MLP_CUDA(cudaMemcpyAsync(grad_out, p->grad, sizeof(float) * (size_t)p->n, cudaMemcpyDeviceToHost, p->stream));
     MLP_CUDA(cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, p->stream));
     MLP_CUDA(cudaStreamSynchronize(p->stream));
+    if (mlp_error(p)) return set_last_error(MMF_ERR_CUDA, "MLP training kernel: an asynchronous-copy or MMA wait gave up");
     if (loss_out) *loss_out = l / (float)B;
     return MMF_OK;
 }
@@ -240,8 +254,17 @@ int mmf_mlp_train_batch(mmf_mlp *p, const void *d_X, const unsigned char *d_y, i
         float l = 0.0f;
         MLP_CUDA(cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, p->stream));
         MLP_CUDA(cudaStreamSynchronize(p->stream));
+        if (mlp_error(p)) return set_last_error(MMF_ERR_CUDA, "MLP training kernel: an asynchronous-copy or MMA wait gave up");
         *loss_out = l / (float)B;
     }
+    return MMF_OK;
+}
+
+int mmf_mlp_set_wait_limits(mmf_mlp *p, int64_t wait_limit, int64_t probe_limit)
+{
+    if (!p || wait_limit < 1 || probe_limit < 0) return set_last_error(MMF_ERR_ARG, "bad argument");
+    p->lim.wait = wait_limit;
+    p->lim.probe = probe_limit;
     return MMF_OK;
 }
 
@@ -258,7 +281,9 @@ int mmf_mlp_predict(mmf_mlp *p, const void *d_X, int64_t n, float *d_prob)
                                   : launch_infer<2, MLP_SRC_X>(p, gp, nullptr, (const __nv_bfloat16 *)d_X, 0.5f, d_prob, nullptr, p->stream);
     MLP_CUDA(e);
     MLP_CUDA(cudaStreamSynchronize(p->stream));
-    if (mlp_error(p)) return set_last_error(MMF_ERR_CUDA, "MLP kernel: an asynchronous-copy or MMA wait gave up");
+    if (const int we = mlp_error(p))
+        return set_last_error(MMF_ERR_CUDA, we == 3 ? "MLP kernel: the probe wait gave up (nothing in flight)"
+                                                    : "MLP kernel: an asynchronous-copy or MMA wait gave up");
     return MMF_OK;
 }
 

@@ -269,13 +269,26 @@ __device__ __forceinline__ bool tile_in_row(const GridParams &gp, long long tile
     return g0 % gp.n[0] + MLP_TILE <= gp.n[0] && g0 + MLP_TILE <= gp.plane;
 }
 
+// Iteration limits of the inference kernel's mbarrier waits.  'wait' bounds
+// every wait on the weights' bulk copies and on the MMA completions.  'probe'
+// > 0 makes each CTA first wait on a barrier that nothing completes, for that
+// many iterations, before it issues any copy or MMA: the wait gives up with
+// nothing in flight, so the kernel's give-up path (error flag, TMEM freed,
+// early return) can be exercised on a GPU without leaving work behind.
+struct WaitLimits {
+    long long wait;
+    long long probe;
+};
+
 // Fused features + MLP over the cells of a grid (persistent, one 128-cell tile
 // per iteration).  prob (nullable) receives y, flags (nullable) y > threshold.
-// Returns through *err a non-zero code if an MMA completion wait gave up.
+// Sets *err when a wait gave up: 1 an MMA completion, 2 the weights' copies,
+// 3 the probe barrier (WaitLimits).
 template <int DIM, int SRC>
 __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const double *U, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
-                                                           unsigned char *flags, int *err, BatchGeom bg)
+                                                           unsigned char *flags, int *err, BatchGeom bg,
+                                                           WaitLimits lim)
 {
     constexpr int KP = mlp_kpad(DIM);
     extern __shared__ __align__(1024) unsigned char dyn[];
@@ -286,6 +299,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     float *sQ = reinterpret_cast<float *>(sW2 + MLP_H * MLP_H);          // primitive strip of a tile
     __shared__ __align__(8) uint64_t mbar_mma;
     __shared__ __align__(8) uint64_t mbar_load;
+    __shared__ __align__(8) uint64_t mbar_probe;
     __shared__ uint32_t tmem_base;
     __shared__ float s_b1[MLP_H], s_b2[MLP_H], s_w3[MLP_H];
     __shared__ int s_fail;
@@ -294,6 +308,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar_mma)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar_load)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar_probe)));
         asm volatile("fence.mbarrier_init.release.cluster;");
         s_fail = 0;
     }
@@ -308,9 +323,15 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     __syncthreads();
+    if (lim.probe > 0) {
+        // nothing arrives on mbar_probe and no copy or MMA has been issued yet
+        const bool ok = __syncthreads_and(mbar_wait(&mbar_probe, 0, lim.probe));
+        if (!ok && tid == 0) { atomicExch(err, 3); s_fail = 1; }
+        __syncthreads();
+    }
     // weights: two bulk asynchronous copies completing on mbar_load
     const uint32_t w1_bytes = MLP_H * KP * 2, w2_bytes = MLP_H * MLP_H * 2;
-    if (tid == 0) {
+    if (tid == 0 && !s_fail) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&mbar_load)),
                      "r"(w1_bytes + w2_bytes));
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -320,7 +341,8 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
                          smem_addr(sW2)),
                      "l"(w.w2c), "r"(w2_bytes), "r"(smem_addr(&mbar_load)));
     }
-    const bool loaded = __syncthreads_and(mbar_wait(&mbar_load, 0, 1ll << 22));
+    const bool probe_failed = s_fail != 0;
+    const bool loaded = probe_failed || __syncthreads_and(mbar_wait(&mbar_load, 0, lim.wait));
     if (!loaded && tid == 0) { atomicExch(err, 2); s_fail = 1; }
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();
@@ -368,7 +390,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
             }
             umma_commit(&mbar_mma);
         }
-        bool ok = mbar_wait(&mbar_mma, phase, 1ll << 22);
+        bool ok = mbar_wait(&mbar_mma, phase, lim.wait);
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (!__syncthreads_and(ok)) { if (tid == 0) { atomicExch(err, 1); s_fail = 1; } break; }
@@ -394,7 +416,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
             }
             umma_commit(&mbar_mma);
         }
-        ok = mbar_wait(&mbar_mma, phase, 1ll << 22);
+        ok = mbar_wait(&mbar_mma, phase, lim.wait);
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (!__syncthreads_and(ok)) { if (tid == 0) { atomicExch(err, 1); s_fail = 1; } break; }

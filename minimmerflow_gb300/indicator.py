@@ -54,6 +54,11 @@ class TroubledCellMLP:
         capi.check(self._lib.mmf_mlp_train_batch(self._p, capi.ptr(d_X), capi.ptr(d_y), batch, lr, C.byref(loss)))
         return loss.value
 
+    def set_wait_limits(self, wait_limit=1 << 22, probe_limit=0):
+        """Iteration limits of the inference kernel's barrier waits
+        (mmf_mlp_set_wait_limits)."""
+        capi.check(self._lib.mmf_mlp_set_wait_limits(self._p, wait_limit, probe_limit))
+
     def predict(self, d_X, d_prob):
         capi.check(self._lib.mmf_mlp_predict(self._p, capi.ptr(d_X), d_X.shape[0], capi.ptr(d_prob)))
 

@@ -66,6 +66,36 @@ def test_tcgen05_predict_matches_oracle(mmf, dim, n):
     assert np.abs(prob.cpu().numpy() - ref).max() < 2e-4
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_bounded_wait_gives_up_and_reports(mmf, dim):
+    """Every mbarrier wait of the tcgen05 inference kernel is bounded.  With a
+    probe limit, each CTA first waits on a barrier that nothing completes,
+    before any bulk copy or MMA is issued, so the wait runs out with nothing
+    in flight: the kernel must return (freeing its tensor memory), set its
+    error flag, and the entry point must report it.  The same context then
+    predicts correctly again once the probe is off.  (The reference only logs
+    bad states, src/euler.cpp:94-101; it has no waits to bound.)"""
+    import torch
+    from minimmerflow_gb300.indicator import TroubledCellMLP
+    mo = mlp_oracle()
+    mlp = TroubledCellMLP(dim=dim, seed=3)
+    real = 135 if dim == 3 else 45
+    n = 1000
+    X, dX = rand_features(n, mlp.width, real, 8)
+    prob = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
+    mlp.set_wait_limits(wait_limit=1 << 22, probe_limit=8)
+    with pytest.raises(mmf.capi.MMFError) as ei:
+        mlp.predict(dX, prob)
+    assert ei.value.code == mmf.capi.MMF_ERR_CUDA
+    assert "probe wait gave up" in str(ei.value)
+    assert bool((prob == -1.0).all())   # no tile ran
+    torch.cuda.synchronize()            # the context is still usable
+    mlp.set_wait_limits()
+    mlp.predict(dX, prob)
+    ref, _ = mo.forward(mlp.params().astype(np.float64), X, mlp.width)
+    assert np.abs(prob.cpu().numpy() - ref).max() < 2e-4
+
+
 def numpy_features(U, dim, n, periodic):
     """Features of every cell (x fastest), FP64 restatement of the kernel's definition."""
     g = 1.4
