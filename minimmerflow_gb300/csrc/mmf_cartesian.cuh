@@ -523,10 +523,18 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
 // bottom edges by two more warps; every other face is evaluated once, by the
 // cell on its low side: x faces move between lanes by shuffles, y faces go
 // through shared memory, z faces stay in registers along the march.
-// Barriers per plane: records published, faces published, shared memory free.
+//
+// Two barriers per plane: (A) the plane's records are in shared memory,
+// (B) its faces are.  The next plane's records and halo records are written
+// after (B), during the update of this plane: every read of the record slots
+// happens between (A) and (B), and every read of the face slots between (B)
+// and the next (A), so no third barrier is needed.  The extra passes sit on
+// different SM sub-partitions (warp w runs on sub-partition w % 4): the halo
+// records on 1, 2 and 3 (between (B) and (A)), the edge faces on 0 and 3
+// (between (A) and (B)).
 constexpr int TILE_X = 32, TILE_Y = 16;
-constexpr int TW_TOP = 4, TW_BOT = 9, TW_SIDE = 14;   // warps of the halo-record passes
-constexpr int TW_LEFTF = 3, TW_BOTF = 15;             // warps of the edge-face passes
+constexpr int TW_TOP = 5, TW_BOT = 6, TW_SIDE = 7;   // warps of the halo-record passes
+constexpr int TW_BOTF = 4, TW_LEFTF = 3;             // warps of the edge-face passes
 
 template <int NV>
 struct SmemTile {
@@ -540,6 +548,49 @@ struct SmemTile {
     double Fl[NV][TILE_Y];           // x face on the tile's left edge, row w
     double Fb[NV][32];               // y face on the tile's bottom edge, column l
 };
+
+// The halo records of plane z (the x or y part their faces use), by the
+// three halo warps.
+template <class A, int STAGE>
+__device__ __forceinline__ void tile_halo_records(const StageArgs &sa, const GridParams &gp, const StepScalars &sc,
+                                                  SmemTile<A::NVAR> &sm, int w, int l, int x0, int y0, int z)
+{
+    constexpr int NV = A::NVAR;
+    if (w == TW_TOP || w == TW_BOT) {
+        RecOf<A, 3> h;
+        load_record<A, STAGE, 3>(sa, gp, sc, x0 + l, w == TW_TOP ? y0 + TILE_Y : y0 - 1, z, h, nullptr);
+        if (w == TW_TOP) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.yc[TILE_Y][k][l] = h.c[k]; sm.yf[TILE_Y][k][l] = h.f[1][k]; }
+            sm.ylam[TILE_Y][l] = h.lam[1];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.bc[k][l] = h.c[k]; sm.bf[k][l] = h.f[1][k]; }
+            sm.blam[l] = h.lam[1];
+        }
+    } else if (w == TW_SIDE) {
+        const int side = l >> 4, r = l & 15;
+        RecOf<A, 3> h;
+        load_record<A, STAGE, 3>(sa, gp, sc, side ? x0 + TILE_X : x0 - 1, y0 + r, z, h, nullptr);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.xc[side][k][r] = h.c[k]; sm.xf[side][k][r] = h.f[0][k]; }
+        sm.xlam[side][r] = h.lam[0];
+    }
+}
+
+// This row's y side, and column 0's x side, of record r.
+template <int NV>
+__device__ __forceinline__ void tile_publish(SmemTile<NV> &sm, const CellRecV<3, NV> &r, int w, int l)
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { sm.yc[w][k][l] = r.c[k]; sm.yf[w][k][l] = r.f[1][k]; }
+    sm.ylam[w][l] = r.lam[1];
+    if (l == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.c0[k][w] = r.c[k]; sm.f0[k][w] = r.f[0][k]; }
+        sm.lam0[w] = r.lam[0];
+    }
+}
 
 template <class A, int STAGE>
 __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParams gp, StageArgs sa)
@@ -577,38 +628,10 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
         const double lz = face_dir<A, 3>(nxt, cur, 2, Fzlo);
         if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
     }
+    tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z0);
+    tile_publish<NV>(sm, cur, w, l);
     for (int z = z0; z < z1; ++z) {
-        // halo records of plane z (the part of the record their faces use)
-        if (w == TW_TOP || w == TW_BOT) {
-            RecOf<A, 3> h;
-            load_record<A, STAGE, 3>(sa, gp, sc, x, w == TW_TOP ? y0 + TILE_Y : y0 - 1, z, h, nullptr);
-            if (w == TW_TOP) {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) { sm.yc[TILE_Y][k][l] = h.c[k]; sm.yf[TILE_Y][k][l] = h.f[1][k]; }
-                sm.ylam[TILE_Y][l] = h.lam[1];
-            } else {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) { sm.bc[k][l] = h.c[k]; sm.bf[k][l] = h.f[1][k]; }
-                sm.blam[l] = h.lam[1];
-            }
-        } else if (w == TW_SIDE) {
-            const int side = l >> 4, r = l & 15;
-            RecOf<A, 3> h;
-            load_record<A, STAGE, 3>(sa, gp, sc, side ? x0 + TILE_X : x0 - 1, y0 + r, z, h, nullptr);
-#pragma unroll
-            for (int k = 0; k < NV; ++k) { sm.xc[side][k][r] = h.c[k]; sm.xf[side][k][r] = h.f[0][k]; }
-            sm.xlam[side][r] = h.lam[0];
-        }
-        // this row's y side, and column 0's x side
-#pragma unroll
-        for (int k = 0; k < NV; ++k) { sm.yc[w][k][l] = cur.c[k]; sm.yf[w][k][l] = cur.f[1][k]; }
-        sm.ylam[w][l] = cur.lam[1];
-        if (l == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) { sm.c0[k][w] = cur.c[k]; sm.f0[k][w] = cur.f[0][k]; }
-            sm.lam0[w] = cur.lam[0];
-        }
-        __syncthreads();
+        __syncthreads();   // (A) records of plane z
         // x face on the right: the next lane, or the right halo column
         {
             double cR[NV], fR[NV];
@@ -658,7 +681,7 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
             for (int k = 0; k < NV; ++k) sm.Fb[k][l] = F[k];
             if (STAGE <= STAGE_1 && x < nx && y0 < ny) lmax = max_nonneg(lmax, le);
         }
-        __syncthreads();
+        __syncthreads();   // (B) faces of plane z
         // the faces below and on the left: the previous lane / row, or the tile edge
         const int wb = (w > 0) ? w - 1 : 0;
 #pragma unroll
@@ -678,7 +701,11 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
             store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
                                    acc, cur.c);
         }
-        __syncthreads();
+        // records of plane z+1 for the next (A)
+        if (z + 1 < z1) {
+            tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z + 1);
+            tile_publish<NV>(sm, nxt, w, l);
+        }
         cur = nxt;
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];

@@ -6,8 +6,9 @@
 //
 //   slopes_kernel       computePolynomials: MUSCL slopes per direction and
 //                       conservative field with the monotonised-central (MC)
-//                       limiter sigma = minmod(2a, 2b, (a+b)/2), a = U_i - U_{i-1},
-//                       b = U_{i+1} - U_i (border neighbours are the ghost states
+//                       limiter sigma = minmod(2a, 2b, c), a = U_i - U_{i-1},
+//                       b = U_{i+1} - U_i, c = (U_{i+1} - U_{i-1}) / 2 the
+//                       central slope (border neighbours are the ghost states
 //                       of euler.cpp:261-376), then a positivity fallback: if any
 //                       face state U +- sigma/2 has rho <= 0 or p <= 0 the cell
 //                       falls back to order 1.  A per-cell flag (limit / central)
@@ -45,7 +46,7 @@ struct O2Args {
     long long cell0, cell1;  // slopes of grid cells [cell0, cell1) (a band of rows or planes)
 };
 
-// a*b <= 0 -> 0; else sign(a) min(2|a|, 2|b|, |a+b|/2)  (oracle orc_compute_polynomials)
+// a*b <= 0 -> 0; else sign(a) min(2|a|, 2|b|, |central|)  (oracle orc_compute_polynomials)
 template <class A>
 __device__ __forceinline__ double mc_slope(double a, double b, double central)
 {
@@ -278,11 +279,13 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
         }
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const double a = uc[k] - ul[k];
-            const double b = ur[k] - uc[k];
-            const double central = IsExact<A>::value ? 0.5 * (a + b) : half_ftz(a + b);
+            // the central slope is one difference; the one-sided ones are
+            // only needed where the limiter runs
+            const double central = IsExact<A>::value ? 0.5 * (ur[k] - ul[k]) : half_ftz(ur[k] - ul[k]);
             double sl = central;
             if (limit) {
+                const double a = uc[k] - ul[k];
+                const double b = ur[k] - uc[k];
                 // the activity is only recorded where a caller keeps it (stage 1)
                 if (IsExact<A>::value) {
                     sl = mc_slope<A>(a, b, central);

@@ -448,7 +448,7 @@ void orc_compute_polynomials(const orc_mesh *m, int problem, int order, const do
             for (int k = 0; k < NF; ++k) {
                 double a = uc[k] - ul[k];
                 double b = ur[k] - uc[k];
-                double central = 0.5 * (a + b);
+                double central = 0.5 * (ur[k] - ul[k]);   /* one difference: (U+ - U-) / 2 */
                 double s = central;
                 if (limit) {
                     if (a * b <= 0.0) s = 0.0;
