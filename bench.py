@@ -607,6 +607,36 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
     return dict(out=out, diff=diff, errs=errs, ncell=case.ncells, trained_here=trained_here)
 
 
+def run_mlp_train(args, local):
+    """Training steps of the troubled-cell MLP (3D: 135-64-64-1) on seeded
+    synthetic features in [-1, 1] (BF16) and labels: each step is one
+    mmf_mlp_train_batch (forward, backward and weight-gradient GEMMs on the
+    tcgen05 tensor cores, then Adam) over a mini-batch; CUDA events around
+    each step on the MLP's stream."""
+    import torch
+    from minimmerflow_gb300.indicator import TroubledCellMLP
+
+    torch.cuda.set_device(local)
+    mlp = TroubledCellMLP(dim=3, seed=args.seed)
+    batch = args.batch
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+    X = (torch.rand((batch, mlp.width), generator=g, device="cuda") * 2 - 1)
+    X[:, 135:] = 0
+    dX = X.to(torch.bfloat16).view(torch.int16).contiguous()
+    dy = (torch.rand(batch, generator=g, device="cuda") < 0.3).to(torch.uint8)
+    for _ in range(args.warmup):
+        mlp.train_batch(dX, dy, batch, 1e-3)
+    torch.cuda.synchronize()
+    durs = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        mlp.train_batch(dX, dy, batch, 1e-3)   # returns after the loss is read back (stream synchronised)
+        durs.append(time.perf_counter() - t0)
+    flop = 2.0 * batch * (mlp.width * 64 + 64 * 64) * 3   # forward, input gradient and weight gradient GEMMs
+    mlp.close()
+    return {"value": batch * args.steps / sum(durs), "durs": durs, "flop_per_step": flop, "batch": batch}
+
+
 def make_case(args):
     import minimmerflow_gb300 as mmf
     if args.workload == "sod2d":
@@ -820,16 +850,19 @@ def run_ours(args, world, rank, local, dist, case=None, steps=None, warmup=None,
     hv = host.numpy()
     hv[:] = U0
     s.time_setup(case.cfl, 0.0, case.t_end, limit)
-    k_e2e = max(3, min(steps, 50 if case.ncells < 4e6 else 5))
+    k_e2e = max(5, min(steps, 50 if case.ncells < 4e6 else 9))
     for _ in range(2):
         s.advance_host(hv, 1)
     hv[:] = U0
     s.time_setup(case.cfl, 0.0, case.t_end, -1 if limit < 0 else 10 ** 9)
-    t0 = time.perf_counter()
+    calls = []
     for _ in range(k_e2e):
+        t0 = time.perf_counter()
         s.advance_host(hv, 1)
-    e2e_s = time.perf_counter() - t0
-    e2e_val = world * ncell * k_e2e / e2e_s
+        calls.append(time.perf_counter() - t0)
+    # the median call: one host round trip competes with other traffic on the
+    # host link, and single calls of the large 3D state vary by +-15%
+    e2e_val = world * ncell / statistics.median(calls)
     s.close()
     return dict(value=value, total=total, clocks=clock_rec, launches=launches, st_mean=st_mean, dominant=dominant,
                 e2e=e2e_val, ncell=ncell, case=case, tuned=tuned, durs=durs, sustained=sustained)
@@ -843,7 +876,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "reference"])
     ap.add_argument("--workload", default="sod2d",
-                    choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned", "facelist"])
+                    choices=["sod2d", "vortex3d_z", "vortex3d_x", "batched", "sod3d_learned", "facelist", "mlp_train"])
+    ap.add_argument("--batch", type=int, default=16384, help="mlp_train: samples per training step")
     ap.add_argument("--threshold", type=float, default=0.0, help="0 = the calibrated threshold of the weights file")
     ap.add_argument("--learned", action="store_true")
     ap.add_argument("--cfl-order2", type=float, default=0.4)
@@ -885,6 +919,21 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.workload == "mlp_train":
+        r = run_mlp_train(args, local)
+        if rank != 0:
+            return
+        line = {"metric": "training samples/s", "value": r["value"], "unit": "samples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["durs"]) / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 x bf16 -> f32",
+                "data": "synthetic",
+                "config": {"workload": ("troubled-cell MLP 135-64-64-1 (GELU, sigmoid, BCE, Adam), mini-batch %d "
+                                        "of seeded features in [-1, 1]" % r["batch"])},
+                "step_times": step_stats(r["durs"]),
+                "gemm_tflops": r["flop_per_step"] * args.steps / sum(r["durs"]) / 1e12,
+                "timing": "host clock around each mmf_mlp_train_batch, which synchronises its stream"}
+        print(json.dumps(line))
+        return
     if args.workload == "facelist":
         r = run_facelist(args, world, rank, local, dist)
         if rank != 0:

@@ -308,11 +308,12 @@ int mmf_mlp_set_params(mmf_mlp *mlp, const float *params, int64_t n);
 int mmf_mlp_gradients(mmf_mlp *mlp, const void *d_X, const unsigned char *d_y, int64_t B, float *grad, float *loss);
 /* One Adam step on a batch. */
 int mmf_mlp_train_batch(mmf_mlp *mlp, const void *d_X, const unsigned char *d_y, int64_t B, float lr, float *loss);
-/* Iteration limits of the inference kernel's mbarrier waits (default 2^22
- * and 0).  Every wait on the weights' bulk copies and on the MMA completions
- * gives up after wait_limit polls: the kernel then sets its error flag, frees
- * its tensor memory and returns, and the entry point that launched it returns
- * MMF_ERR_CUDA.  probe_limit > 0 makes every CTA first wait on a barrier that
+/* Iteration limits of the tcgen05 kernels' mbarrier waits (default 2^22
+ * and 0).  Every wait of the inference and training kernels on the weights'
+ * bulk copies and on the MMA completions gives up after wait_limit polls: the
+ * kernel then sets its error flag, frees its tensor memory and returns, and
+ * the entry point that launched it returns MMF_ERR_CUDA.  probe_limit > 0
+ * makes every CTA of the inference kernel first wait on a barrier that
  * nothing completes, before any copy or MMA is issued: a test of that path
  * with nothing in flight.  No reference counterpart (the reference only logs
  * bad states, src/euler.cpp:94-101). */

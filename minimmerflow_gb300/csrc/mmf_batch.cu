@@ -20,7 +20,8 @@
 namespace mmf {
 int set_last_error(int code, const char *msg);
 cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
-                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s);
+                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s,
+                                float *Q);
 int mlp_dim(const mmf_mlp *p);
 }
 using namespace mmf;
@@ -95,6 +96,7 @@ struct mmf_batch {
     long long *d_offsets = nullptr;
     mmf_mlp *indicator = nullptr;
     float ind_threshold = 0.5f;
+    float *ind_q = nullptr;   // the indicator's FP32 primitive planes (5 x total)
 
     void drop_graphs()
     {
@@ -128,9 +130,9 @@ struct mmf_batch {
         cudaError_t e;
         if (order == 2) {
             if (indicator) {
-                ++launches;
+                launches += 2;   // primitives, then features + MLP
                 if ((e = mlp_indicator_batch(indicator, cases, d_offsets, ncases, total, U, ind_threshold, lim_flag,
-                                             stream)) != cudaSuccess)
+                                             stream, ind_q)) != cudaSuccess)
                     return e;
             }
             if ((e = o2(BO2_SLOPES, STAGE_1, U, nullptr)) != cudaSuccess) return e;
@@ -145,7 +147,7 @@ struct mmf_batch {
         if ((e = stage(STAGE_2, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U);
     }
-    int launches_per_step() const { return order == 2 ? (indicator ? 8 : 7) : 3; }
+    int launches_per_step() const { return order == 2 ? (indicator ? 9 : 7) : 3; }
 };
 
 static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
@@ -315,7 +317,7 @@ int mmf_batch_destroy(mmf_batch *b)
     b->drop_graphs();
     cudaFree(b->U); cudaFree(b->R); cudaFree(b->W); cudaFree(b->aos); cudaFree(b->ctrl); cudaFree(b->flag);
     cudaFree(b->cases); cudaFree(b->item_case);
-    cudaFree(b->S); cudaFree(b->lim_flag); cudaFree(b->lim_active); cudaFree(b->d_offsets);
+    cudaFree(b->S); cudaFree(b->lim_flag); cudaFree(b->lim_active); cudaFree(b->d_offsets); cudaFree(b->ind_q);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return MMF_OK;
@@ -454,6 +456,10 @@ int mmf_batch_set_indicator(mmf_batch *b, mmf_mlp *mlp, float threshold)
     if (rc) return rc;
     if (b->order != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
     if (mlp && mlp_dim(mlp) != 2) return set_last_error(MMF_ERR_ARG, "batched cases need a 2D indicator");
+    if (mlp && !b->ind_q) {
+        const cudaError_t e = cudaMalloc(&b->ind_q, sizeof(float) * 5 * (size_t)b->total);
+        if (e != cudaSuccess) return set_last_error(MMF_ERR_NOMEM, cudaGetErrorString(e));
+    }
     b->indicator = mlp;
     b->ind_threshold = threshold;
     b->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;

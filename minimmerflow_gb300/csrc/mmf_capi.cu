@@ -126,7 +126,7 @@ int check_grid(const mmf_grid *grid)
 }
 // mmf_mlp.cu
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s);
+                          unsigned char *flags, cudaStream_t s, float *Q);
 cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s);
 int mlp_dim(const mmf_mlp *p);
 int mlp_error(mmf_mlp *p);
@@ -215,7 +215,7 @@ int mmf_destroy(mmf_ctx *c)
     if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
     cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
-    cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active); cudaFree(c->steplog);
+    cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active); cudaFree(c->steplog); cudaFree(c->ind_q);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
@@ -488,11 +488,13 @@ int mmf_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold, float *prob, unsign
     if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
     if (mlp_dim(mlp) != c->grid.dim) return fail(MMF_ERR_ARG, "MLP dimension differs from the mesh");
     const long long n = c->gp.plane;
-    float *dprob = nullptr;
+    float *dprob = nullptr, *q = nullptr;
     if (prob) MMF_CUDA(cudaMalloc(&dprob, sizeof(float) * (size_t)n));
-    ++c->launches;
-    cudaError_t e = mlp_indicator(mlp, c->gp, c->U, threshold, dprob, c->lim_flag, c->stream);
+    cudaError_t e = cudaMalloc(&q, sizeof(float) * 5 * (size_t)n);
+    c->launches += 2;
+    if (e == cudaSuccess) e = mlp_indicator(mlp, c->gp, c->U, threshold, dprob, c->lim_flag, c->stream, q);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(q);
     if (e == cudaSuccess && mlp_error(mlp)) { cudaFree(dprob); return fail(MMF_ERR_CUDA, "indicator: a wait gave up"); }
     if (e == cudaSuccess && prob) {
         std::vector<float> tmp((size_t)n);
@@ -543,6 +545,7 @@ int mmf_set_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold)
     if (rc) return rc;
     if (mlp && c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
     if (mlp && mlp_dim(mlp) != c->grid.dim) return fail(MMF_ERR_ARG, "MLP dimension differs from the mesh");
+    if (mlp && !c->ind_q) MMF_CUDA(cudaMalloc(&c->ind_q, sizeof(float) * 5 * (size_t)c->gp.plane));
     c->indicator = mlp;
     c->ind_threshold = threshold;
     c->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;

@@ -10,7 +10,7 @@
 
 namespace mmf {
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s);
+                          unsigned char *flags, cudaStream_t s, float *Q);
 }
 
 using namespace mmf;
@@ -39,6 +39,7 @@ struct mmf_ctx {
     int limit_mode = LIMIT_ALL;
     mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
     float ind_threshold = 0.5f;
+    float *ind_q = nullptr;             // the indicator's FP32 primitive planes (5 x plane)
     // pipelined host round trip (mmf_advance_host): a copy stream, one event
     // per band and direction, pinned host words for the flag and the control block
     static constexpr int MAX_BANDS = 8;
@@ -96,8 +97,8 @@ struct mmf_ctx {
             // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
             // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
             if (indicator) {
-                ++launches;
-                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream)) != cudaSuccess)
+                launches += 2;   // primitives, then features + MLP
+                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream, ind_q)) != cudaSuccess)
                     return e;
             }
             if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
@@ -112,7 +113,7 @@ struct mmf_ctx {
         if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U, U);
     }
-    int launches_per_step() const { return grid.order == 2 ? (indicator ? 8 : 7) : 3; }
+    int launches_per_step() const { return grid.order == 2 ? (indicator ? 9 : 7) : 3; }
 };
 
 

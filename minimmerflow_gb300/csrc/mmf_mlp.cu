@@ -49,7 +49,7 @@ static int mlp_pack(mmf_mlp *p)
 }
 
 template <int DIM, int SRC>
-static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const double *U, const __nv_bfloat16 *X, float thr,
+static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const float *Q, const __nv_bfloat16 *X, float thr,
                                 float *prob, unsigned char *flags, cudaStream_t s, BatchGeom bg = BatchGeom{nullptr, nullptr, 0})
 {
     const int smem = mlp_infer_smem<DIM>();
@@ -64,29 +64,44 @@ static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const double *
     w.w1c = p->w1c;
     w.w2c = p->w2c;
     w.params = p->params;
-    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, U, X, w, thr, prob, flags, p->err, bg, p->lim);
+    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, Q, X, w, thr, prob, flags, p->err, bg, p->lim);
     return cudaPeekAtLastError();
 }
 
-// Fused features + MLP over a grid state (used by the solver context).
-cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s)
+// The primitive planes Q (5 x n FP32) of SoA FP64 planes U n apart.
+static cudaError_t launch_prims(long long n, const double *U, float *Q, cudaStream_t s)
 {
-    if (p->dim != gp.dim) return cudaErrorInvalidValue;
-    return p->dim == 3 ? launch_infer<3, MLP_SRC_GRID>(p, gp, U, nullptr, thr, prob, flags, s)
-                       : launch_infer<2, MLP_SRC_GRID>(p, gp, U, nullptr, thr, prob, flags, s);
+    const long long b = (n + 255) / 256;
+    mlp_prims_kernel<<<(unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16), 256, 0, s>>>(n, U, Q);
+    return cudaPeekAtLastError();
 }
 
-// Indicator over a packed batch of 2D grids (total cells).
-cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
-                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s)
+// Features + MLP over a grid state (used by the solver context): the
+// primitive planes of U into Q (scratch of 5 x gp.plane floats), then the
+// fused kernel.
+cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
+                          unsigned char *flags, cudaStream_t s, float *Q)
 {
-    if (p->dim != 2) return cudaErrorInvalidValue;
+    if (p->dim != gp.dim || !Q) return cudaErrorInvalidValue;
+    cudaError_t e = launch_prims(gp.plane, U, Q, s);
+    if (e != cudaSuccess) return e;
+    return p->dim == 3 ? launch_infer<3, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, flags, s)
+                       : launch_infer<2, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, flags, s);
+}
+
+// Indicator over a packed batch of 2D grids (total cells; Q: 5 x total floats).
+cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
+                                long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s,
+                                float *Q)
+{
+    if (p->dim != 2 || !Q) return cudaErrorInvalidValue;
     GridParams gp;
     memset(&gp, 0, sizeof(gp));
     gp.dim = 2;
     gp.plane = total;
-    return launch_infer<2, MLP_SRC_BATCH>(p, gp, U, nullptr, thr, nullptr, flags, s, BatchGeom{cases, offsets, ncases});
+    cudaError_t e = launch_prims(total, U, Q, s);
+    if (e != cudaSuccess) return e;
+    return launch_infer<2, MLP_SRC_BATCH>(p, gp, Q, nullptr, thr, nullptr, flags, s, BatchGeom{cases, offsets, ncases});
 }
 
 cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s)

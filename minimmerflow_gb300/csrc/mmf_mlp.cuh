@@ -84,16 +84,22 @@ __device__ __forceinline__ float gelu_grad(float x)
 }
 __device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
-// Primitive variables (rho, u, v, w, p) of the cell at (x, y, z), border wrap or clamp.
-__device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, int x, int y, int z, float *q)
+// Grid index of the stencil cell at (x, y, z): periodic borders wrap, the
+// others clamp (zero gradient).
+__device__ __forceinline__ long long stencil_index(const GridParams &gp, int x, int y, int z)
 {
     const bool px = gp.bc_lo[0] == BC_PERIODIC, py = gp.bc_lo[1] == BC_PERIODIC, pz = gp.bc_lo[2] == BC_PERIODIC;
     const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
     x = x < 0 ? (px ? nx - 1 : 0) : (x >= nx ? (px ? 0 : nx - 1) : x);
     y = y < 0 ? (py ? ny - 1 : 0) : (y >= ny ? (py ? 0 : ny - 1) : y);
     z = z < 0 ? (pz ? nz - 1 : 0) : (z >= nz ? (pz ? 0 : nz - 1) : z);
-    const long long g = (long long)x + (long long)nx * ((long long)y + (long long)ny * z);
-    const long long n = gp.plane;
+    return (long long)x + (long long)nx * ((long long)y + (long long)ny * z);
+}
+
+// Primitive variables (rho, u, v, w, p) in FP32 of cell g of SoA FP64 planes
+// n apart.
+__device__ __forceinline__ void prim_of(const double *U, long long n, long long g, float *q)
+{
     const float rho = (float)__ldg(U + g);
     const float ri = 1.0f / rho;
     const float u = (float)__ldg(U + n + g) * ri, v = (float)__ldg(U + 2 * n + g) * ri,
@@ -104,6 +110,34 @@ __device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, i
     q[2] = v;
     q[3] = w;
     q[4] = (float)(GAMMA - 1.0) * (E - 0.5f * rho * (u * u + v * v + w * w));
+}
+
+// Primitive variables of the stencil cell at (x, y, z), from the state.
+__device__ __forceinline__ void prim_at(const double *U, const GridParams &gp, int x, int y, int z, float *q)
+{
+    prim_of(U, gp.plane, stencil_index(gp, x, y, z), q);
+}
+
+// ... and from the primitive planes of mlp_prims_kernel (the same values).
+__device__ __forceinline__ void prim_q_at(const float *Q, const GridParams &gp, int x, int y, int z, float *q)
+{
+    const long long g = stencil_index(gp, x, y, z);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] = __ldg(Q + v * gp.plane + g);
+}
+
+// The primitive variables of cells [0, n) of SoA FP64 planes n apart, as FP32
+// SoA planes n apart: each cell converted once per indicator run, instead of
+// once per stencil (or strip) that contains it.
+__global__ void __launch_bounds__(256) mlp_prims_kernel(long long n, const double *__restrict__ U,
+                                                        float *__restrict__ Q)
+{
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        float q[5];
+        prim_of(U, n, g, q);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Q[v * n + g] = q[v];
+    }
 }
 
 template <int DIM, class Put>
@@ -127,20 +161,37 @@ __device__ __forceinline__ void cell_features(const double *U, const GridParams 
     stencil_features<DIM>(q, put);
 }
 
+// The KPAD features of grid cell g from the primitive planes Q.
+template <int DIM, class Put>
+__device__ __forceinline__ void cell_features_q(const float *Q, const GridParams &gp, long long g, Put put)
+{
+    constexpr int NS = DIM == 3 ? 27 : 9;
+    int x, y, z;
+    cell_coords(gp, g, x, y, z);
+    if (DIM == 2) z = 0;
+    float q[NS][5];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
+        prim_q_at(Q, gp, x + dx, y + dy, z + dz, q[s]);
+    }
+    stencil_features<DIM>(q, put);
+}
+
 // Primitive strip of a tile of MLP_TILE cells that lie in one grid row
 // (x0 .. x0 + MLP_TILE - 1 at row y, plane z): for each of the 3^(DIM-1)
 // (dy, dz) rows of the stencil, the MLP_TILE + 2 cells x0 - 1 .. x0 + MLP_TILE,
 // each converted once (instead of once per stencil that contains it).
 // sQ[(r * (MLP_TILE + 2) + j) * 5 + v], r = (dy + 1) + 3 (dz + 1).
 template <int DIM>
-__device__ __forceinline__ void tile_strip(const double *U, const GridParams &gp, int x0, int y, int z, int tid, float *sQ)
+__device__ __forceinline__ void tile_strip(const float *Q, const GridParams &gp, int x0, int y, int z, int tid, float *sQ)
 {
     constexpr int NR = DIM == 3 ? 9 : 3;
-#pragma unroll 1
+#pragma unroll
     for (int r = 0; r < NR; ++r) {
         const int dy = r % 3 - 1, dz = DIM == 3 ? r / 3 - 1 : 0;
-        prim_at(U, gp, x0 - 1 + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + tid) * 5);
-        if (tid < 2) prim_at(U, gp, x0 - 1 + MLP_TILE + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + MLP_TILE + tid) * 5);
+        prim_q_at(Q, gp, x0 - 1 + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + tid) * 5);
+        if (tid < 2) prim_q_at(Q, gp, x0 - 1 + MLP_TILE + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + MLP_TILE + tid) * 5);
     }
 }
 
@@ -285,7 +336,7 @@ struct WaitLimits {
 // Sets *err when a wait gave up: 1 an MMA completion, 2 the weights' copies,
 // 3 the probe barrier (WaitLimits).
 template <int DIM, int SRC>
-__global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const double *U, const __nv_bfloat16 *X,
+__global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
                                                            unsigned char *flags, int *err, BatchGeom bg,
                                                            WaitLimits lim)
@@ -362,17 +413,17 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
         } else if (g < gp.plane && SRC == MLP_SRC_BATCH) {
             const int c = case_of(bg, g);
             const long long off = bg.offsets[c];
-            cell_features<DIM>(U + off, bg.cases[c].gp, g - off,
-                               [&](int k, float v) { pk.put(k, v); });
+            cell_features_q<DIM>(Q + off, bg.cases[c].gp, g - off,
+                                 [&](int k, float v) { pk.put(k, v); });
         } else if (SRC == MLP_SRC_GRID && tile_in_row(gp, tile)) {
             const long long g0 = tile * MLP_TILE;
             const int nx = gp.n[0];
-            tile_strip<DIM>(U, gp, (int)(g0 % nx), (int)((g0 / nx) % gp.n[1]),
+            tile_strip<DIM>(Q, gp, (int)(g0 % nx), (int)((g0 / nx) % gp.n[1]),
                             DIM == 3 ? (int)(g0 / ((long long)nx * gp.n[1])) : 0, tid, sQ);
             __syncthreads();
             strip_features<DIM>(sQ, tid, [&](int k, float v) { pk.put(k, v); });
         } else if (g < gp.plane) {
-            cell_features<DIM>(U, gp, g, [&](int k, float v) { pk.put(k, v); });
+            cell_features_q<DIM>(Q, gp, g, [&](int k, float v) { pk.put(k, v); });
         } else {
 #pragma unroll
             for (int k = 0; k < KP; ++k) pk.put(k, 0.0f);
