@@ -10,7 +10,8 @@
 //             velocities, a_c the centre sound speed); borders wrap (periodic)
 //             or clamp (zero gradient)
 //   network   h1 = GELU(W1 x + b1) (64), h2 = GELU(W2 h1 + b2) (64),
-//             y = sigmoid(w3 . h2 + b3); BF16 operands, FP32 accumulation
+//             y = sigmoid(w3 . h2 + b3); BF16 operands, FP32 accumulation;
+//             GELU in its tanh form (gelu below)
 //
 // Inference (mlp_infer_kernel) is one fused, persistent tcgen05 kernel per
 // 128-cell tile: the 128 threads of a CTA compute one cell's features each
@@ -77,10 +78,21 @@ struct RowPacker {
     }
 };
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))),
+// written as x sigma(z) with z = 2 sqrt(2/pi) (x + 0.044715 x^3): one
+// exponential and one reciprocal per value (the network applies 128 per cell).
+constexpr float GELU_C = 1.5957691216057308f;   // 2 sqrt(2 / pi)
+__device__ __forceinline__ float gelu(float x)
+{
+    const float z = GELU_C * fmaf(0.044715f * x, x * x, x);
+    return __fdividef(x, 1.0f + __expf(-z));
+}
 __device__ __forceinline__ float gelu_grad(float x)
 {
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * __expf(-0.5f * x * x);
+    const float x2 = x * x;
+    const float z = GELU_C * fmaf(0.044715f * x, x2, x);
+    const float s = __fdividef(1.0f, 1.0f + __expf(-z));
+    return fmaf(x * s * (1.0f - s), GELU_C * fmaf(3.0f * 0.044715f, x2, 1.0f), s);
 }
 __device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
@@ -97,19 +109,22 @@ __device__ __forceinline__ long long stencil_index(const GridParams &gp, int x, 
 }
 
 // Primitive variables (rho, u, v, w, p) in FP32 of cell g of SoA FP64 planes
-// n apart.
+// n apart.  Every operation is an explicitly rounded intrinsic, so the bits do
+// not depend on where the compiler inlines this (the indicator's primitive
+// planes and the training features must agree).
 __device__ __forceinline__ void prim_of(const double *U, long long n, long long g, float *q)
 {
     const float rho = (float)__ldg(U + g);
-    const float ri = 1.0f / rho;
-    const float u = (float)__ldg(U + n + g) * ri, v = (float)__ldg(U + 2 * n + g) * ri,
-                w = (float)__ldg(U + 3 * n + g) * ri;
+    const float ri = __fdiv_rn(1.0f, rho);
+    const float u = __fmul_rn((float)__ldg(U + n + g), ri), v = __fmul_rn((float)__ldg(U + 2 * n + g), ri),
+                w = __fmul_rn((float)__ldg(U + 3 * n + g), ri);
     const float E = (float)__ldg(U + 4 * n + g);
+    const float s2 = __fmaf_rn(w, w, __fmaf_rn(v, v, __fmul_rn(u, u)));
     q[0] = rho;
     q[1] = u;
     q[2] = v;
     q[3] = w;
-    q[4] = (float)(GAMMA - 1.0) * (E - 0.5f * rho * (u * u + v * v + w * w));
+    q[4] = __fmul_rn((float)(GAMMA - 1.0), __fsub_rn(E, __fmul_rn(__fmul_rn(0.5f, rho), s2)));
 }
 
 // Primitive variables of the stencil cell at (x, y, z), from the state.

@@ -34,15 +34,22 @@ def unpack(params, kpad):
     return W1, b1, W2, b2, w3, b3
 
 
-_erf = np.vectorize(math.erf)
+GELU_C = 2.0 * math.sqrt(2.0 / math.pi)
+
+
+def _sigmoid(z):
+    with np.errstate(over="ignore"):
+        return 1.0 / (1.0 + np.exp(-z))
 
 
 def gelu(x):
-    return 0.5 * x * (1.0 + _erf(x / math.sqrt(2.0)))
+    """GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) = x sigmoid(z)."""
+    return x * _sigmoid(GELU_C * (x + 0.044715 * x ** 3))
 
 
 def gelu_grad(x):
-    return 0.5 * (1.0 + _erf(x / math.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / math.sqrt(2.0 * math.pi)
+    s = _sigmoid(GELU_C * (x + 0.044715 * x ** 3))
+    return s + x * s * (1.0 - s) * GELU_C * (1.0 + 3.0 * 0.044715 * x * x)
 
 
 def forward(params, X, kpad):
