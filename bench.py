@@ -27,6 +27,9 @@ The default line also carries (each with its own workload description):
   sod3d_learned   3D radial Sod 256^3, order 2, learned / plain / no cell flagged;
   dropin_binding  the reference loop through three mmf_compute_rhs host calls
                   per step;
+  equal_error_vortex  time to solution at equal L1 error on the 2D vortex:
+                  the plain order-1 path on 1024^2 against the learned order 2
+                  on the coarsest mesh that is as accurate;
   sustained       about 1.5 s of back-to-back steps with clock samples;
   step_times      the spread of the K timed steps.
 
@@ -476,6 +479,60 @@ def run_sweep_comparison(args, local, steps, warmup):
     out["learned_over_plain_concurrent"] = out["learned"]["value"] / out["plain_concurrent_streams"]["value"]
     out["learned_over_batched_limited"] = out["learned"]["value"] / out["limited"]["value"]
     out["ceiling_no_cell_flagged_over_limited"] = out["no_cell_flagged"]["value"] / out["limited"]["value"]
+    return out
+
+
+def run_equal_error(args, local, t_end=2.0, plain_n=1024):
+    """Time to solution at equal accuracy on the 2D isentropic vortex (beta 5,
+    [-5,5]^2, periodic, free stream rho = u = v = p = 1) to t = 2: the plain
+    FP64 path (order 1, the reference's method, CFL 0.5) on a plain_n^2 mesh,
+    and the order-2 solver with the learned indicator (CFL 0.4) on the
+    coarsest mesh of a ladder whose L1 density error against the exact
+    solution (src/main.cpp:550-561) is at most 1.01 times the plain path's.
+    The state is on the device; the host clock brackets one mmf_advance of
+    exactly the steps the run takes to t = 2 (counted by an untimed run).  The
+    fully limited order 2 on the same coarse mesh is timed beside it."""
+    import minimmerflow_gb300 as mmf
+    from minimmerflow_gb300 import indicator, train_indicator
+
+    mlp, thr = train_indicator.load(2, device=local)
+    if mlp is None:
+        mlp, _, thr = train_indicator.train(2, samples=1_000_000, epochs=8, log=None)
+
+    def solve(n, order, cfl, learned):
+        case = mmf.problem.vortex(2, n, steps=-1)
+        case.t_end = t_end
+        with case.solver(arith=args.arith, device=local, order=order) as s:
+            if learned:
+                indicator.use_indicator(s, mlp, thr)
+            # an untimed run gives the step count (and builds the step graphs);
+            # the timed run then enqueues exactly that many steps
+            s.upload(case.initial_state())
+            s.time_setup(cfl, 0.0, t_end, -1)
+            _, steps = s.advance(10 ** 7)
+            s.upload(case.initial_state())
+            s.time_setup(cfl, 0.0, t_end, -1)
+            t0 = time.perf_counter()
+            t, done = s.advance(steps)
+            secs = time.perf_counter() - t0
+            assert done == steps and t == t_end
+            err = case.l1_density_error(s.download(), t)
+        return {"n": n, "order": order, "cfl": cfl, "steps": steps, "t": t, "l1_density_error": err,
+                "seconds": secs, "cell_updates": n * n * steps}
+
+    plain = solve(plain_n, 1, 0.5, False)
+    learned = None
+    for n in (32, 40, 48, 56, 64, 80, 96, 128, 192, 256):
+        r = solve(n, 2, 0.4, True)
+        if r["l1_density_error"] <= 1.01 * plain["l1_density_error"]:
+            learned = r
+            break
+    out = {"plain_order1": plain, "learned_order2": learned}
+    if learned is not None:
+        out["limited_order2_same_mesh"] = solve(learned["n"], 2, 0.4, False)
+        out["time_ratio_plain_over_learned"] = plain["seconds"] / learned["seconds"]
+        out["plain_equivalent_cell_updates_per_s"] = plain["cell_updates"] / learned["seconds"]
+    mlp.close()
     return out
 
 
@@ -1118,6 +1175,7 @@ def main():
         guarded("batched_learned", sweep)
         guarded("sod3d_learned", learned3d)
         guarded("dropin_binding", lambda: run_dropin(args, local, max(3, min(args.steps, 5))))
+        guarded("equal_error_vortex", lambda: run_equal_error(args, local))
     if not args.no_cpu and args.workload == "sod2d":
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
     print(json.dumps(line))

@@ -13,14 +13,17 @@
 //             y = sigmoid(w3 . h2 + b3); BF16 operands, FP32 accumulation;
 //             GELU in its tanh form (gelu below)
 //
-// Inference (mlp_infer_kernel) is one fused, persistent tcgen05 kernel per
-// 128-cell tile: the 128 threads of a CTA compute one cell's features each
-// and store them as BF16 in the shared-memory operand layout; one thread
-// issues tcgen05.mma into a TMEM accumulator (layer 1: 9 MMAs of K 16 for
-// 3D), the tile's h1 comes back with tcgen05.ld, goes through GELU into a
-// second shared operand, layer 2 accumulates into a second TMEM region, and
-// each thread finishes its own row (GELU, dot with w3, sigmoid).  Weights are
-// staged once per CTA with bulk asynchronous copies (cp.async.bulk).
+// Inference is two kernels.  mlp_prims_kernel converts every cell's state to
+// FP32 primitives once.  mlp_infer_kernel is one fused, persistent tcgen05
+// kernel per 128-cell tile, three CTAs per SM: the 128 threads of a CTA
+// compute one cell's features each from the primitive planes and store them
+// as BF16 in the shared-memory operand layout; one thread issues tcgen05.mma
+// into a TMEM accumulator (layer 1: 9 MMAs of K 16 for 3D), the tile's h1
+// comes back with tcgen05.ld and goes through GELU into the layer-2 operand,
+// which reuses the layer-1 operand's shared memory once that MMA has
+// completed; layer 2 accumulates into a second TMEM region, and each thread
+// finishes its own row (GELU, dot with w3, sigmoid).  Weights are staged once
+// per CTA with bulk asynchronous copies (cp.async.bulk).
 //
 // Shared operand layout (K-major, no swizzle): 8-row x 16-byte core matrices;
 // core matrix (row block rb, k block kb) at byte (kb * ROWS/8 + rb) * 128, row
@@ -40,9 +43,13 @@ namespace mmf {
 
 constexpr int MLP_H = 64;            // hidden width
 constexpr int MLP_TILE = 128;        // cells per tcgen05 tile (M)
+constexpr int MLP_CTAS_PER_SM = 3;   // inference CTAs per SM (shared memory, registers, 3 x 128 TMEM columns)
 
 __host__ __device__ constexpr int mlp_kin(int dim) { return dim == 3 ? 135 : 45; }
 __host__ __device__ constexpr int mlp_kpad(int dim) { return dim == 3 ? 144 : 48; }
+// elements of the inference kernel's first operand region: X (128 x KPAD),
+// later H (128 x 64)
+__host__ __device__ constexpr int mlp_operand_elems(int dim) { return 128 * (mlp_kpad(dim) > 64 ? mlp_kpad(dim) : 64); }
 
 // Flat FP32 parameter vector: W1 [64][KPAD], b1 [64], W2 [64][64], b2 [64], w3 [64], b3 [1]
 __host__ __device__ constexpr long long mlp_off_b1(int dim) { return (long long)MLP_H * mlp_kpad(dim); }
@@ -67,12 +74,17 @@ struct RowPacker {
     __nv_bfloat16 *base;
     int row, rows;
     uint32_t w[4];
+    float pend = 0.0f;   // the even element of the pair being formed
+    // Elements go in pairs through one two-way conversion (round to nearest
+    // even, as the one-way conversion rounds).
     __device__ __forceinline__ void put(int k, float v)
     {
-        const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v));
-        const int j = (k & 7) >> 1;
-        if (k & 1) w[j] |= h << 16;
-        else w[j] = h;
+        if ((k & 1) == 0) {
+            pend = v;
+        } else {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(pend, v);   // .x = element k - 1
+            w[(k & 7) >> 1] = *reinterpret_cast<const uint32_t *>(&h);
+        }
         if ((k & 7) == 7)
             *reinterpret_cast<uint4 *>(base + core_offset(row, k - 7, rows)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -155,8 +167,8 @@ __global__ void __launch_bounds__(256) mlp_prims_kernel(long long n, const doubl
     }
 }
 
-template <int DIM, class Put>
-__device__ __forceinline__ void stencil_features(float (*q)[5], Put put);
+template <int DIM, class Get, class Put>
+__device__ __forceinline__ void stencil_features(Get get, Put put);
 
 // The KPAD features of grid cell g (FP32), written through 'put(k, value)'.
 // Stencil cell s is at (dx, dy, dz) = (s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1).
@@ -173,10 +185,12 @@ __device__ __forceinline__ void cell_features(const double *U, const GridParams 
         const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
         prim_at(U, gp, x + dx, y + dy, z + dz, q[s]);
     }
-    stencil_features<DIM>(q, put);
+    stencil_features<DIM>([&](int s, int v) { return q[s][v]; }, put);
 }
 
-// The KPAD features of grid cell g from the primitive planes Q.
+// The KPAD features of grid cell g from the primitive planes Q: the
+// stencil's cell indices once, then one variable at a time (the loads hit L1
+// and L2, where the neighbouring cells' stencils brought the same values).
 template <int DIM, class Put>
 __device__ __forceinline__ void cell_features_q(const float *Q, const GridParams &gp, long long g, Put put)
 {
@@ -184,62 +198,38 @@ __device__ __forceinline__ void cell_features_q(const float *Q, const GridParams
     int x, y, z;
     cell_coords(gp, g, x, y, z);
     if (DIM == 2) z = 0;
-    float q[NS][5];
+    long long idx[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
-        prim_q_at(Q, gp, x + dx, y + dy, z + dz, q[s]);
+        idx[s] = stencil_index(gp, x + dx, y + dy, z + dz);
     }
-    stencil_features<DIM>(q, put);
+    stencil_features<DIM>([&](int s, int v) { return __ldg(Q + v * gp.plane + idx[s]); }, put);
 }
 
-// Primitive strip of a tile of MLP_TILE cells that lie in one grid row
-// (x0 .. x0 + MLP_TILE - 1 at row y, plane z): for each of the 3^(DIM-1)
-// (dy, dz) rows of the stencil, the MLP_TILE + 2 cells x0 - 1 .. x0 + MLP_TILE,
-// each converted once (instead of once per stencil that contains it).
-// sQ[(r * (MLP_TILE + 2) + j) * 5 + v], r = (dy + 1) + 3 (dz + 1).
-template <int DIM>
-__device__ __forceinline__ void tile_strip(const float *Q, const GridParams &gp, int x0, int y, int z, int tid, float *sQ)
-{
-    constexpr int NR = DIM == 3 ? 9 : 3;
-#pragma unroll
-    for (int r = 0; r < NR; ++r) {
-        const int dy = r % 3 - 1, dz = DIM == 3 ? r / 3 - 1 : 0;
-        prim_q_at(Q, gp, x0 - 1 + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + tid) * 5);
-        if (tid < 2) prim_q_at(Q, gp, x0 - 1 + MLP_TILE + tid, y + dy, z + dz, sQ + (r * (MLP_TILE + 2) + MLP_TILE + tid) * 5);
-    }
-}
-
-// The features of the tile's cell 'tid' from the strip.
-template <int DIM, class Put>
-__device__ __forceinline__ void strip_features(const float *sQ, int tid, Put put)
-{
-    constexpr int NS = DIM == 3 ? 27 : 9;
-    float q[NS][5];
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-#pragma unroll
-        for (int v = 0; v < 5; ++v) q[s][v] = sQ[((s / 3) * (MLP_TILE + 2) + tid + s % 3) * 5 + v];
-    stencil_features<DIM>(q, put);
-}
-
-// Normalised stencil differences of the primitives q[s][v] (FP32).
-template <int DIM, class Put>
-__device__ __forceinline__ void stencil_features(float (*q)[5], Put put)
+// Normalised stencil differences of the primitives get(s, v) (FP32), one
+// variable at a time (the stencil's values of one variable are the only ones
+// held at once).  Every operation is explicitly rounded: the features are the
+// same bits wherever this is inlined (training data and inference).
+template <int DIM, class Get, class Put>
+__device__ __forceinline__ void stencil_features(Get get, Put put)
 {
     constexpr int NS = DIM == 3 ? 27 : 9;
     constexpr int C = DIM == 3 ? 13 : 4;   // centre of the stencil
-    const float a_c = sqrtf(fmaxf((float)GAMMA * q[C][4] / q[C][0], 0.0f));
+    const float a_c = sqrtf(fmaxf(__fdiv_rn(__fmul_rn((float)GAMMA, get(C, 4)), get(C, 0)), 0.0f));
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-        const float c = q[C][v];
+        float q[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) q[s] = get(s, v);
+        const float c = q[C];
         float m = 0.0f;
 #pragma unroll
-        for (int s = 0; s < NS; ++s) m = fmaxf(m, fabsf(q[s][v] - c));
-        const float eps = (v == 0 || v == 4) ? 1e-4f * fabsf(c) : 1e-4f * a_c;
-        const float inv = 1.0f / (m + eps + 1e-30f);
+        for (int s = 0; s < NS; ++s) m = fmaxf(m, fabsf(__fsub_rn(q[s], c)));
+        const float eps = __fmul_rn(1e-4f, (v == 0 || v == 4) ? fabsf(c) : a_c);
+        const float inv = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(m, eps), 1e-30f));
 #pragma unroll
-        for (int s = 0; s < NS; ++s) put(v * NS + s, (q[s][v] - c) * inv);
+        for (int s = 0; s < NS; ++s) put(v * NS + s, __fmul_rn(__fsub_rn(q[s], c), inv));
     }
 #pragma unroll
     for (int k = 5 * NS; k < mlp_kpad(DIM); ++k) put(k, 0.0f);
@@ -328,13 +318,6 @@ struct MlpDev {
     const float *params;        // FP32 parameters (biases, w3, b3 are read from here)
 };
 
-// The tile's MLP_TILE cells lie in one grid row (the strip path applies).
-__device__ __forceinline__ bool tile_in_row(const GridParams &gp, long long tile)
-{
-    const long long g0 = tile * MLP_TILE;
-    return g0 % gp.n[0] + MLP_TILE <= gp.n[0] && g0 + MLP_TILE <= gp.plane;
-}
-
 // Iteration limits of the inference kernel's mbarrier waits.  'wait' bounds
 // every wait on the weights' bulk copies and on the MMA completions.  'probe'
 // > 0 makes each CTA first wait on a barrier that nothing completes, for that
@@ -351,24 +334,26 @@ struct WaitLimits {
 // Sets *err when a wait gave up: 1 an MMA completion, 2 the weights' copies,
 // 3 the probe barrier (WaitLimits).
 template <int DIM, int SRC>
-__global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
+__global__ void __launch_bounds__(128, MLP_CTAS_PER_SM) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
                                                            unsigned char *flags, int *err, BatchGeom bg,
                                                            WaitLimits lim)
 {
     constexpr int KP = mlp_kpad(DIM);
     extern __shared__ __align__(1024) unsigned char dyn[];
-    __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(dyn);          // 128 x KP
-    __nv_bfloat16 *sW1 = sX + MLP_TILE * KP;                             // 64 x KP
-    __nv_bfloat16 *sH = sW1 + MLP_H * KP;                                // 128 x 64
-    __nv_bfloat16 *sW2 = sH + MLP_TILE * MLP_H;                          // 64 x 64
-    float *sQ = reinterpret_cast<float *>(sW2 + MLP_H * MLP_H);          // primitive strip of a tile
+    // the layer-1 operand X (128 x KP) and, once its MMA has completed, the
+    // layer-2 operand H (128 x 64) share the first region
+    __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(dyn);
+    __nv_bfloat16 *sH = sX;
+    __nv_bfloat16 *sW1 = sX + mlp_operand_elems(DIM);                    // 64 x KP
+    __nv_bfloat16 *sW2 = sW1 + MLP_H * KP;                               // 64 x 64
     __shared__ __align__(8) uint64_t mbar_mma;
     __shared__ __align__(8) uint64_t mbar_load;
     __shared__ __align__(8) uint64_t mbar_probe;
     __shared__ uint32_t tmem_base;
     __shared__ float s_b1[MLP_H], s_b2[MLP_H], s_w3[MLP_H];
     __shared__ int s_fail;
+    __shared__ int s_case;
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -422,21 +407,21 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
     for (long long tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
         const long long g = tile * MLP_TILE + tid;
         RowPacker pk{sX, tid, MLP_TILE, {0u, 0u, 0u, 0u}};
+        if (SRC == MLP_SRC_BATCH) {
+            // the tile's first case, once per tile (a case has at least 32 x 32
+            // cells, so a tile of 128 cells meets at most two)
+            if (tid == 0) s_case = case_of(bg, tile * MLP_TILE < gp.plane ? tile * MLP_TILE : gp.plane - 1);
+            __syncthreads();
+        }
         // features of this thread's cell -> BF16 operand rows
         if (g < gp.plane && SRC == MLP_SRC_X) {
             for (int k = 0; k < KP; ++k) sX[core_offset(tid, k, MLP_TILE)] = X[g * KP + k];
         } else if (g < gp.plane && SRC == MLP_SRC_BATCH) {
-            const int c = case_of(bg, g);
+            int c = s_case;
+            while (c + 1 < bg.ncases && bg.offsets[c + 1] <= g) ++c;
             const long long off = bg.offsets[c];
             cell_features_q<DIM>(Q + off, bg.cases[c].gp, g - off,
                                  [&](int k, float v) { pk.put(k, v); });
-        } else if (SRC == MLP_SRC_GRID && tile_in_row(gp, tile)) {
-            const long long g0 = tile * MLP_TILE;
-            const int nx = gp.n[0];
-            tile_strip<DIM>(Q, gp, (int)(g0 % nx), (int)((g0 / nx) % gp.n[1]),
-                            DIM == 3 ? (int)(g0 / ((long long)nx * gp.n[1])) : 0, tid, sQ);
-            __syncthreads();
-            strip_features<DIM>(sQ, tid, [&](int k, float v) { pk.put(k, v); });
         } else if (g < gp.plane) {
             cell_features_q<DIM>(Q, gp, g, [&](int k, float v) { pk.put(k, v); });
         } else {
@@ -511,8 +496,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(GridParams gp, const 
 template <int DIM>
 constexpr int mlp_infer_smem()
 {
-    return (MLP_TILE * mlp_kpad(DIM) + MLP_H * mlp_kpad(DIM) + MLP_TILE * MLP_H + MLP_H * MLP_H) * 2 +
-           (DIM == 3 ? 9 : 3) * (MLP_TILE + 2) * 5 * 4;
+    return (mlp_operand_elems(DIM) + MLP_H * mlp_kpad(DIM) + MLP_H * MLP_H) * 2;
 }
 
 } // namespace mmf
