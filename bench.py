@@ -489,8 +489,9 @@ def run_equal_error(args, local, t_end=2.0, plain_n=1024):
     and the order-2 solver with the learned indicator (CFL 0.4) on the
     coarsest mesh of a ladder whose L1 density error against the exact
     solution (src/main.cpp:550-561) is at most 1.01 times the plain path's.
-    The state is on the device; the host clock brackets one mmf_advance of
-    exactly the steps the run takes to t = 2 (counted by an untimed run).  The
+    The state is on the device; the decomposition is tuned per mesh; the host
+    clock brackets one mmf_advance of exactly the steps the run takes to t = 2
+    (counted by an untimed run).  The
     fully limited order 2 on the same coarse mesh is timed beside it."""
     import minimmerflow_gb300 as mmf
     from minimmerflow_gb300 import indicator, train_indicator
@@ -505,10 +506,13 @@ def run_equal_error(args, local, t_end=2.0, plain_n=1024):
         with case.solver(arith=args.arith, device=local, order=order) as s:
             if learned:
                 indicator.use_indicator(s, mlp, thr)
-            # an untimed run gives the step count (and builds the step graphs);
-            # the timed run then enqueues exactly that many steps
+            # an untimed run gives the step count (and builds the step graphs),
+            # after the decomposition is tuned for this mesh (a 56^2 mesh has
+            # work for a few warps only with the default chunks); the timed run
+            # then enqueues exactly that many steps
             s.upload(case.initial_state())
             s.time_setup(cfl, 0.0, t_end, -1)
+            s.autotune(trial_steps=2)
             _, steps = s.advance(10 ** 7)
             s.upload(case.initial_state())
             s.time_setup(cfl, 0.0, t_end, -1)

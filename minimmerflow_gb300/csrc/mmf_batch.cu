@@ -187,7 +187,7 @@ static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
     BATCH_CUDA(cudaStreamSynchronize(b->stream));
     b->nitems = (int)item_case.size();
     b->chunk = chunk;
-    const int maxb = batch_max_blocks_per_sm(b->arith, b->w_zero);
+    const int maxb = batch_max_blocks_per_sm(b->arith, b->w_zero, b->order);
     b->blocks_per_sm = (blocks_per_sm > 0) ? std::min(blocks_per_sm, maxb) : maxb;
     b->blocks = b->sms * b->blocks_per_sm;
     b->drop_graphs();
@@ -492,7 +492,7 @@ int mmf_batch_autotune(mmf_batch *b, int trial_steps, int *chunk_out, int *block
     BATCH_CUDA(cudaMemcpyAsync(b->aos, b->U, bytes, cudaMemcpyDeviceToDevice, b->stream));
     BATCH_CUDA(cudaMemcpyAsync(saved.data(), b->ctrl, sizeof(Ctrl) * saved.size(), cudaMemcpyDeviceToHost, b->stream));
     BATCH_CUDA(cudaStreamSynchronize(b->stream));
-    const int maxb = batch_max_blocks_per_sm(b->arith, b->w_zero);
+    const int maxb = batch_max_blocks_per_sm(b->arith, b->w_zero, b->order);
     const int chunks[] = {8, 16, 32, 64};
     std::vector<int> bps;
     for (int v = maxb; v >= 1 && (int)bps.size() < 3; v = v / 2) bps.push_back(v);

@@ -154,9 +154,16 @@ __global__ void __launch_bounds__(128) form_w1_batch_kernel(const CaseDesc *__re
     });
 }
 
+// Minimum resident blocks per SM the order-2 batch march is compiled for:
+// the four-field fast variant (2D states with zero z-momentum, the batched
+// sweep's) gets the 128 registers the single-grid march reaches on its own,
+// so that four persistent blocks of four warps fit on an SM.
+template <class A> struct O2BatchMinBlocks { static constexpr int value = 1; };
+template <> struct O2BatchMinBlocks<FastArithT<4>> { static constexpr int value = 4; };
+
 // order-2 stage march of every item
 template <class A, int STAGE>
-__global__ void __launch_bounds__(128) stage2d_o2_batch_kernel(const CaseDesc *__restrict__ cases,
+__global__ void __launch_bounds__(128, O2BatchMinBlocks<A>::value) stage2d_o2_batch_kernel(const CaseDesc *__restrict__ cases,
                                                                const int *__restrict__ item_case, int nitems,
                                                                Ctrl *cctrl, StageArgs base, const double *state,
                                                                const double *S)
@@ -181,6 +188,19 @@ __global__ void __launch_bounds__(128) stage2d_o2_batch_kernel(const CaseDesc *_
 }
 
 enum BatchO2Op { BO2_SLOPES = 0, BO2_FORM_W1 = 1, BO2_STAGE = 2 };
+
+// Resident blocks per SM of the order-2 batch launches (the least of the
+// stage marches and the slopes, which share the persistent grid).
+template <class A>
+inline int batch_o2_blocks_per_sm()
+{
+    int nb = 1 << 20, v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_1>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_2>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_3>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, slopes_batch_kernel<A>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
+    return (nb > 0 && nb < (1 << 20)) ? nb : 1;
+}
 
 template <class A>
 inline cudaError_t launch_batch_o2(int op, int stage, const CaseDesc *cases, const int *item_case, int nitems,
@@ -215,6 +235,6 @@ cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item
                                const StageArgs &base, int blocks, cudaStream_t s);
 cudaError_t launch_batch_fast(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
                               const StageArgs &base, int blocks, cudaStream_t s, bool w_zero);
-int batch_max_blocks_per_sm(int arith, bool w_zero);
+int batch_max_blocks_per_sm(int arith, bool w_zero, int order);
 
 } // namespace mmf

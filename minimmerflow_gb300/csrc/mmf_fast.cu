@@ -38,9 +38,10 @@ cudaError_t launch_batch_o2_fast(int op, int stage, const CaseDesc *cases, const
     return launch_batch_o2<FastArith>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
 }
 
-int batch_max_blocks_per_sm(int arith, bool w_zero)
+int batch_max_blocks_per_sm(int arith, bool w_zero, int order)
 {
-    if (arith == 0) return batch_max_blocks_per_sm_exact();
+    if (arith == 0) return batch_max_blocks_per_sm_exact(order);
+    if (order == 2) return w_zero ? batch_o2_blocks_per_sm<FastArith2DW0>() : batch_o2_blocks_per_sm<FastArith>();
     return w_zero ? batch_blocks_per_sm<FastArith2DW0>() : batch_blocks_per_sm<FastArith>();
 }
 
