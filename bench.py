@@ -373,8 +373,10 @@ def run_sweep_comparison(args, local, steps, warmup):
     # "no_cell_flagged": the flagged mode with the flags as created (all zero),
     # central slopes and the positivity fallback on every cell -- what the
     # learned path would cost with an indicator that is free and flags nothing
-    for mode in ("no_cell_flagged", "limited", "learned"):
-        b.set_indicator(mlp if mode == "learned" else None, thr)
+    # "learned_every_2nd_step": the indicator every second step, flags dilated by one cell
+    for mode in ("no_cell_flagged", "limited", "learned", "learned_every_2nd_step"):
+        b.set_indicator(mlp if mode.startswith("learned") else None, thr,
+                        period=2 if mode == "learned_every_2nd_step" else 1)
         if mode == "no_cell_flagged":
             b.set_limiter("flagged")
         b.upload(packed)
@@ -402,22 +404,23 @@ def run_sweep_comparison(args, local, steps, warmup):
     del packed
 
     # accuracy: vortex cases against the exact solution after 20 steps
-    ratios, el_sum, ep_sum = [], 0.0, 0.0
-    for i, c in enumerate(cases):
-        if c.problem != mmf.problem.VORTEX_XY:
-            continue
-        # each case and each run has its own time after 20 steps (its own dt sequence)
-        ep = c.l1_density_error(finals["limited"][0][i], finals["limited"][1][i])
-        el = c.l1_density_error(finals["learned"][0][i], finals["learned"][1][i])
-        ratios.append(el / ep)
-        el_sum += el
-        ep_sum += ep
-    out["accuracy"] = {"vortex_cases": len(ratios), "steps": 20,
-                       "l1_error_ratio_learned_over_plain": {"mean": float(np.mean(ratios)),
-                                                             "max": float(np.max(ratios)),
-                                                             "sum_over_cases": el_sum / ep_sum},
+    out["accuracy"] = {"steps": 20,
                        "plain": "the batched order 2 with every cell limited, bit-identical per case to a "
                                 "single-case context (tests/test_gpu_batch.py)"}
+    for mode in ("learned", "learned_every_2nd_step"):
+        ratios, el_sum, ep_sum = [], 0.0, 0.0
+        for i, c in enumerate(cases):
+            if c.problem != mmf.problem.VORTEX_XY:
+                continue
+            # each case and each run has its own time after 20 steps (its own dt sequence)
+            ep = c.l1_density_error(finals["limited"][0][i], finals["limited"][1][i])
+            el = c.l1_density_error(finals[mode][0][i], finals[mode][1][i])
+            ratios.append(el / ep)
+            el_sum += el
+            ep_sum += ep
+        out["accuracy"]["vortex_cases"] = len(ratios)
+        out["accuracy"]["l1_error_ratio_%s_over_plain" % mode] = {
+            "mean": float(np.mean(ratios)), "max": float(np.max(ratios)), "sum_over_cases": el_sum / ep_sum}
     del finals
 
     # plain per-case contexts on concurrent streams, and one after another
@@ -478,6 +481,10 @@ def run_sweep_comparison(args, local, steps, warmup):
                                        "sweep's total cells" % (n1, n1)}
     out["learned_over_plain_concurrent"] = out["learned"]["value"] / out["plain_concurrent_streams"]["value"]
     out["learned_over_batched_limited"] = out["learned"]["value"] / out["limited"]["value"]
+    out["learned_every_2nd_step_over_plain_concurrent"] = (out["learned_every_2nd_step"]["value"]
+                                                           / out["plain_concurrent_streams"]["value"])
+    out["learned_every_2nd_step_over_batched_limited"] = (out["learned_every_2nd_step"]["value"]
+                                                          / out["limited"]["value"])
     out["ceiling_no_cell_flagged_over_limited"] = out["no_cell_flagged"]["value"] / out["limited"]["value"]
     return out
 
@@ -620,10 +627,10 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
     U0 = case.initial_state()
     out = {}
     finals = {}
-    for mode in ("plain", "learned", "no_cell_flagged"):
+    for mode in ("plain", "learned", "no_cell_flagged", "learned_every_2nd_step"):
         s = case.solver(arith=args.arith, device=local, order=2)
-        if mode == "learned":
-            indicator.use_indicator(s, mlp, args.threshold)
+        if mode.startswith("learned"):
+            indicator.use_indicator(s, mlp, args.threshold, period=2 if mode == "learned_every_2nd_step" else 1)
         if mode == "no_cell_flagged":
             s.set_limiter("flagged", flags=np.zeros(case.ncells, dtype=np.uint8))
         stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
@@ -650,19 +657,21 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
                          launches=s.launch_count - launches0, status=s.status(), step_times=step_stats(durs))
         if mode != "no_cell_flagged":
             finals[mode] = s.download()
-        if mode == "learned":
+        if mode.startswith("learned"):
             _, flags = indicator.run_indicator(s, mlp, args.threshold)
             out[mode]["limited_fraction"] = float(flags.mean())
         s.close()
-    diff = float(np.abs(finals["learned"][:, 0] - finals["plain"][:, 0]).sum() / np.abs(finals["plain"][:, 0]).sum())
+    rho_plain = np.abs(finals["plain"][:, 0]).sum()
+    diff = {m: float(np.abs(finals[m][:, 0] - finals["plain"][:, 0]).sum() / rho_plain)
+            for m in ("learned", "learned_every_2nd_step")}
     # accuracy against the exact vortex (3D, periodic, 50 steps)
     vc = mmf.problem.vortex(3, args.vortex_n, steps=50)
     V0 = vc.initial_state()
     errs = {}
-    for mode in ("plain", "learned"):
+    for mode in ("plain", "learned", "learned_every_2nd_step"):
         with vc.solver(arith=args.arith, device=local, order=2) as s:
-            if mode == "learned":
-                indicator.use_indicator(s, mlp, args.threshold)
+            if mode.startswith("learned"):
+                indicator.use_indicator(s, mlp, args.threshold, period=2 if mode == "learned_every_2nd_step" else 1)
             V, t, _ = s.run(V0, vc.cfl, max_steps=50)
         errs[mode] = vc.l1_density_error(V, t)
     return dict(out=out, diff=diff, errs=errs, ncell=case.ncells, trained_here=trained_here)
@@ -1166,11 +1175,21 @@ def main():
                                     "ms_per_step": o["no_cell_flagged"]["ms"],
                                     "meaning": "central slopes and the positivity fallback on every cell, no "
                                                "indicator run: the most an indicator could save"},
+                "learned_every_2nd_step": {"value": o["learned_every_2nd_step"]["value"], "unit": metric,
+                                           "ms_per_step": o["learned_every_2nd_step"]["ms"],
+                                           "meaning": "the indicator every second step, its flags dilated by "
+                                                      "one cell"},
                 "learned_over_plain": o["learned"]["value"] / o["plain"]["value"],
+                "learned_every_2nd_step_over_plain": o["learned_every_2nd_step"]["value"] / o["plain"]["value"],
                 "ceiling_no_cell_flagged_over_plain": o["no_cell_flagged"]["value"] / o["plain"]["value"],
                 "limited_fraction_final_state": o["learned"]["limited_fraction"],
+                "limited_fraction_final_state_every_2nd_step": o["learned_every_2nd_step"]["limited_fraction"],
+                "sod_l1_density_difference_vs_plain": rl["diff"],
                 "vortex3d_l1_error": {"plain": rl["errs"]["plain"], "learned": rl["errs"]["learned"],
+                                      "learned_every_2nd_step": rl["errs"]["learned_every_2nd_step"],
                                       "ratio": rl["errs"]["learned"] / rl["errs"]["plain"],
+                                      "ratio_every_2nd_step": rl["errs"]["learned_every_2nd_step"]
+                                                              / rl["errs"]["plain"],
                                       "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2"
                                               % args.vortex_n},
                 "steps": k_extra}

@@ -278,6 +278,8 @@ int mmf_batch_case_info(mmf_batch *batch, int c, double *t, int64_t *steps, unsi
 typedef struct mmf_mlp mmf_mlp;
 int mmf_batch_set_limiter(mmf_batch *batch, int mode);
 int mmf_batch_set_indicator(mmf_batch *batch, mmf_mlp *mlp, float threshold);
+/* mmf_set_indicator_period for a batch (one counter for all its cases). */
+int mmf_batch_set_indicator_period(mmf_batch *batch, int period);
 /* Decomposition: rows per work item and resident blocks per SM (0 = occupancy maximum). */
 int mmf_batch_set_shape(mmf_batch *batch, int chunk, int blocks_per_sm);
 int mmf_batch_get_shape(mmf_batch *batch, int *chunk, int *blocks_per_sm);
@@ -333,6 +335,15 @@ int mmf_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold, float *prob, unsi
 /* From the next step on, every step starts with the indicator on U (inside
  * the step's CUDA graph); mlp = NULL switches it off (limiter back to ALL). */
 int mmf_set_indicator(mmf_ctx *ctx, mmf_mlp *mlp, float threshold);
+/* The indicator runs every 'period' steps (1, the default, or 2).  With 2,
+ * its flags are dilated by one cell (a cell is limited where any cell of its
+ * 3^dim neighbourhood is flagged) and serve the step after as well: at
+ * CFL <= 0.5 a wave moves at most one cell in two steps.  The counter starts
+ * again, so that the next step runs the indicator, whenever the state or the
+ * time control is set (upload, checkpoint, mmf_time_setup, mmf_autotune).
+ * mmf_indicator returns the dilated flags when the period is 2.  No reference
+ * counterpart. */
+int mmf_set_indicator_period(mmf_ctx *ctx, int period);
 
 /* ---- residual without device allocation ------------------------------- */
 /* Largest mesh accepted by mmf_compute_rhs_noalloc. */

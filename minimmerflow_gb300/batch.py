@@ -99,9 +99,12 @@ class BatchEuler:
         m = {"all": capi.LIMIT_ALL, "none": capi.LIMIT_NONE, "flagged": capi.LIMIT_FLAGGED}.get(mode, mode)
         capi.check(self._lib.mmf_batch_set_limiter(self._b, m))
 
-    def set_indicator(self, mlp, threshold):
-        """Order-2 batches: the learned indicator (2D) gates the limiter of every case."""
+    def set_indicator(self, mlp, threshold, period=1):
+        """Order-2 batches: the learned indicator (2D) gates the limiter of every
+        case, every step or every second step (period 2, flags dilated by one cell)."""
         capi.check(self._lib.mmf_batch_set_indicator(self._b, mlp.handle if mlp is not None else None, threshold))
+        if mlp is not None:
+            capi.check(self._lib.mmf_batch_set_indicator_period(self._b, period))
 
     @property
     def stream_handle(self):

@@ -25,10 +25,10 @@ EXPORTS = [
     "mmf_batch_create", "mmf_batch_destroy", "mmf_batch_cell_count", "mmf_batch_launch_count",
     "mmf_batch_get_stream", "mmf_batch_upload", "mmf_batch_download", "mmf_batch_time_setup",
     "mmf_batch_advance_async", "mmf_batch_synchronize", "mmf_batch_case_info", "mmf_batch_set_shape",
-    "mmf_batch_get_shape", "mmf_batch_autotune", "mmf_batch_set_limiter", "mmf_batch_set_indicator",
+    "mmf_batch_get_shape", "mmf_batch_autotune", "mmf_batch_set_limiter", "mmf_batch_set_indicator", "mmf_batch_set_indicator_period",
     "mmf_mlp_create", "mmf_mlp_destroy", "mmf_mlp_num_params", "mmf_mlp_input_width", "mmf_mlp_get_params",
     "mmf_mlp_set_params", "mmf_mlp_set_wait_limits", "mmf_mlp_gradients", "mmf_mlp_train_batch", "mmf_mlp_predict", "mmf_features",
-    "mmf_indicator", "mmf_set_indicator", "mmf_limiter_labels",
+    "mmf_indicator", "mmf_set_indicator", "mmf_set_indicator_period", "mmf_limiter_labels",
     "mmf_umesh_create", "mmf_umesh_destroy", "mmf_umesh_launch_count", "mmf_umesh_upload", "mmf_umesh_download",
     "mmf_umesh_compute_rhs", "mmf_umesh_time_setup", "mmf_umesh_advance",
     "mmf_autotune", "mmf_set_shape", "mmf_set_step_log", "mmf_get_step_log", "mmf_init_state", "mmf_l1_density_error", "mmf_write_vtk", "mmf_save_checkpoint", "mmf_load_checkpoint",
@@ -142,6 +142,8 @@ def load(build_if_missing=True):
     L.mmf_features.argtypes = [_P, _P]
     L.mmf_indicator.argtypes = [_P, _P, C.c_float, _P, _P]
     L.mmf_set_indicator.argtypes = [_P, _P, C.c_float]
+    L.mmf_set_indicator_period.argtypes = [_P, C.c_int]
+    L.mmf_batch_set_indicator_period.argtypes = [_P, C.c_int]
     L.mmf_limiter_labels.argtypes = [_P, _P]
     L.mmf_umesh_create.argtypes = [C.POINTER(UMeshDesc), C.c_int, C.POINTER(_P)]
     L.mmf_umesh_destroy.argtypes = [_P]

@@ -21,7 +21,7 @@ namespace mmf {
 int set_last_error(int code, const char *msg);
 cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
                                 long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s,
-                                float *Q);
+                                float *Q, unsigned char *raw, IndicatorStep is);
 int mlp_dim(const mmf_mlp *p);
 }
 using namespace mmf;
@@ -97,6 +97,15 @@ struct mmf_batch {
     mmf_mlp *indicator = nullptr;
     float ind_threshold = 0.5f;
     float *ind_q = nullptr;   // the indicator's FP32 primitive planes (5 x total)
+    int ind_period = 1;                 // the indicator runs every ind_period steps (1 or 2)
+    int *ind_tick = nullptr;            // device step counter of the period
+    unsigned char *ind_raw = nullptr;   // the network's flags before the dilation (period 2)
+
+    // the next step runs the indicator (after a change of the state or of the time control)
+    void indicator_restart()
+    {
+        if (ind_tick) cudaMemsetAsync(ind_tick, 0, sizeof(int), stream);
+    }
 
     void drop_graphs()
     {
@@ -120,6 +129,8 @@ struct mmf_batch {
         O2Batch ob;
         ob.S = S; ob.flag = lim_flag; ob.active = (op == BO2_SLOPES && st == STAGE_1) ? lim_active : nullptr;
         ob.limit_mode = limit_mode;
+        // a step's stage-1 slopes advance the indicator's step counter
+        ob.tick = (op == BO2_SLOPES && st == STAGE_1 && indicator && ind_period > 1) ? ind_tick : nullptr;
         ++launches;
         return arith == MMF_ARITH_FAST
                    ? launch_batch_o2_fast(op, st, cases, item_case, nitems, ctrl, base, state, ob, W, blocks, stream, w_zero)
@@ -130,9 +141,10 @@ struct mmf_batch {
         cudaError_t e;
         if (order == 2) {
             if (indicator) {
-                launches += 2;   // primitives, then features + MLP
+                launches += ind_period > 1 ? 3 : 2;   // primitives, features + MLP (, dilation)
                 if ((e = mlp_indicator_batch(indicator, cases, d_offsets, ncases, total, U, ind_threshold, lim_flag,
-                                             stream, ind_q)) != cudaSuccess)
+                                             stream, ind_q, ind_period > 1 ? ind_raw : nullptr,
+                                             IndicatorStep{ind_period, ind_tick})) != cudaSuccess)
                     return e;
             }
             if ((e = o2(BO2_SLOPES, STAGE_1, U, nullptr)) != cudaSuccess) return e;
@@ -147,7 +159,7 @@ struct mmf_batch {
         if ((e = stage(STAGE_2, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U);
     }
-    int launches_per_step() const { return order == 2 ? (indicator ? 9 : 7) : 3; }
+    int launches_per_step() const { return order == 2 ? (indicator ? (ind_period > 1 ? 10 : 9) : 7) : 3; }
 };
 
 static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
@@ -318,6 +330,7 @@ int mmf_batch_destroy(mmf_batch *b)
     cudaFree(b->U); cudaFree(b->R); cudaFree(b->W); cudaFree(b->aos); cudaFree(b->ctrl); cudaFree(b->flag);
     cudaFree(b->cases); cudaFree(b->item_case);
     cudaFree(b->S); cudaFree(b->lim_flag); cudaFree(b->lim_active); cudaFree(b->d_offsets); cudaFree(b->ind_q);
+    cudaFree(b->ind_raw); cudaFree(b->ind_tick);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return MMF_OK;
@@ -334,6 +347,7 @@ int mmf_batch_upload(mmf_batch *b, const double *aos, int64_t total)
     if (!aos || total != b->total) return set_last_error(MMF_ERR_ARG, "bad state buffer");
     const size_t bytes = sizeof(double) * NF * (size_t)total;
     BATCH_CUDA(cudaMemcpyAsync(b->aos, aos, bytes, cudaMemcpyHostToDevice, b->stream));
+    b->indicator_restart();
     batch_aos_to_soa<<<(unsigned)((total + 255) / 256), 256, 0, b->stream>>>(b->aos, b->U, total);
     ++b->launches;
     BATCH_CUDA(cudaPeekAtLastError());
@@ -386,6 +400,7 @@ int mmf_batch_time_setup(mmf_batch *b, const double *cfl, const double *t_end, i
         x.max_steps = (max_steps < 0) ? LLONG_MAX : max_steps;
     }
     BATCH_CUDA(cudaMemcpyAsync(b->ctrl, h.data(), sizeof(Ctrl) * h.size(), cudaMemcpyHostToDevice, b->stream));
+    b->indicator_restart();
     BATCH_CUDA(cudaStreamSynchronize(b->stream));
     b->time_ready = true;
     return MMF_OK;
@@ -462,8 +477,27 @@ int mmf_batch_set_indicator(mmf_batch *b, mmf_mlp *mlp, float threshold)
     }
     b->indicator = mlp;
     b->ind_threshold = threshold;
+    b->indicator_restart();
     b->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;
     b->drop_graphs();
+    return MMF_OK;
+}
+
+int mmf_batch_set_indicator_period(mmf_batch *b, int period)
+{
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (period != 1 && period != 2) return set_last_error(MMF_ERR_ARG, "the indicator period must be 1 or 2");
+    if (b->order != 2) return set_last_error(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
+    if (period > 1 && !b->ind_raw) {
+        BATCH_CUDA(cudaMalloc(&b->ind_raw, (size_t)b->total));
+        BATCH_CUDA(cudaMemsetAsync(b->ind_raw, 0, (size_t)b->total, b->stream));
+    }
+    if (period > 1 && !b->ind_tick) BATCH_CUDA(cudaMalloc(&b->ind_tick, sizeof(int)));
+    b->ind_period = period;
+    b->indicator_restart();
+    b->drop_graphs();
+    BATCH_CUDA(cudaStreamSynchronize(b->stream));
     return MMF_OK;
 }
 
@@ -523,6 +557,7 @@ int mmf_batch_autotune(mmf_batch *b, int trial_steps, int *chunk_out, int *block
     cudaEventDestroy(e1);
     cudaMemcpyAsync(b->U, b->aos, bytes, cudaMemcpyDeviceToDevice, b->stream);
     cudaMemcpyAsync(b->ctrl, saved.data(), sizeof(Ctrl) * saved.size(), cudaMemcpyHostToDevice, b->stream);
+    b->indicator_restart();
     BATCH_CUDA(cudaStreamSynchronize(b->stream));
     if (rc) return rc;
     if ((rc = batch_plan(b, best_chunk, best_bps))) return rc;

@@ -83,6 +83,7 @@ struct O2Batch {
     unsigned char *flag;       // packed limiter flags
     unsigned char *active;     // packed limiter activity (nullable)
     int limit_mode;
+    int *tick = nullptr;       // the indicator's step counter, advanced by a step's stage-1 slopes (nullable)
 };
 
 // Walks the item list; for each item of an active case calls body(gp, off, ctrl, seg, chunk).
@@ -107,6 +108,8 @@ __global__ void __launch_bounds__(128) slopes_batch_kernel(const CaseDesc *__res
                                                            const double *state, O2Batch ob, int stage)
 {
     const int lane = threadIdx.x & 31;
+    // no block of this launch reads the counter
+    if (ob.tick && blockIdx.x == 0 && threadIdx.x == 0) *ob.tick += 1;
     for_items(cases, item_case, nitems, cctrl, [&](const GridParams &gp, long long off, Ctrl *ctrl, int seg, int chunk,
                                                    bool) {
         if (!o2_step_active(ctrl, stage)) return;

@@ -126,7 +126,7 @@ int check_grid(const mmf_grid *grid)
 }
 // mmf_mlp.cu
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s, float *Q);
+                          unsigned char *flags, cudaStream_t s, float *Q, unsigned char *raw, IndicatorStep is);
 cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s);
 int mlp_dim(const mmf_mlp *p);
 int mlp_error(mmf_mlp *p);
@@ -216,6 +216,7 @@ int mmf_destroy(mmf_ctx *c)
     cudaFree(c->U); cudaFree(c->R); cudaFree(c->W); cudaFree(c->S); cudaFree(c->aos);
     cudaFree(c->raw_to_cell); cudaFree(c->ctrl); cudaFree(c->rhs_maxeig); cudaFree(c->flag);
     cudaFree(c->Sl); cudaFree(c->lim_flag); cudaFree(c->lim_active); cudaFree(c->steplog); cudaFree(c->ind_q);
+    cudaFree(c->ind_raw); cudaFree(c->ind_tick);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
@@ -276,6 +277,7 @@ static int to_soa(mmf_ctx *c, const double *d_aos, double *soa, int64_t n_raw)
 // plane is identically zero (the graphs are rebuilt when the choice changes).
 static int refresh_w_zero_impl(mmf_ctx *c)
 {
+    c->indicator_restart();   // a new state: the next step runs the indicator
     bool wz = false;
     if (c->gp.dim == 2 && c->grid.arith == MMF_ARITH_FAST) {
         MMF_CUDA(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
@@ -491,8 +493,11 @@ int mmf_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold, float *prob, unsign
     float *dprob = nullptr, *q = nullptr;
     if (prob) MMF_CUDA(cudaMalloc(&dprob, sizeof(float) * (size_t)n));
     cudaError_t e = cudaMalloc(&q, sizeof(float) * 5 * (size_t)n);
-    c->launches += 2;
-    if (e == cudaSuccess) e = mlp_indicator(mlp, c->gp, c->U, threshold, dprob, c->lim_flag, c->stream, q);
+    const bool dilate = c->ind_period > 1 && c->ind_raw;
+    c->launches += dilate ? 3 : 2;
+    if (e == cudaSuccess)
+        e = mlp_indicator(mlp, c->gp, c->U, threshold, dprob, c->lim_flag, c->stream, q, dilate ? c->ind_raw : nullptr,
+                          IndicatorStep{1, nullptr});
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(q);
     if (e == cudaSuccess && mlp_error(mlp)) { cudaFree(dprob); return fail(MMF_ERR_CUDA, "indicator: a wait gave up"); }
@@ -549,8 +554,28 @@ int mmf_set_indicator(mmf_ctx *c, mmf_mlp *mlp, float threshold)
     c->indicator = mlp;
     c->ind_threshold = threshold;
     c->limit_mode = mlp ? LIMIT_FLAGGED : LIMIT_ALL;
+    c->indicator_restart();
     if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
     if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
+    return MMF_OK;
+}
+
+int mmf_set_indicator_period(mmf_ctx *c, int period)
+{
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (period != 1 && period != 2) return fail(MMF_ERR_ARG, "the indicator period must be 1 or 2");
+    if (c->grid.order != 2) return fail(MMF_ERR_UNSUPPORTED, "the indicator drives the order-2 limiter");
+    if (period > 1 && !c->ind_raw) {
+        MMF_CUDA(cudaMalloc(&c->ind_raw, (size_t)c->gp.plane));
+        MMF_CUDA(cudaMemsetAsync(c->ind_raw, 0, (size_t)c->gp.plane, c->stream));
+    }
+    if (period > 1 && !c->ind_tick) MMF_CUDA(cudaMalloc(&c->ind_tick, sizeof(int)));
+    c->ind_period = period;
+    c->indicator_restart();
+    if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
+    if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
+    MMF_CUDA(cudaStreamSynchronize(c->stream));
     return MMF_OK;
 }
 
@@ -588,6 +613,7 @@ int mmf_time_setup(mmf_ctx *c, double cfl, double t, double t_end, int64_t max_s
     h.log = c->steplog;
     h.log_cap = c->steplog_cap;
     MMF_CUDA(cudaMemcpyAsync(c->ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    c->indicator_restart();
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     c->cfl = cfl;
     c->time_ready = true;
@@ -1125,6 +1151,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     MMF_CUDA(e);
     MMF_CUDA(cudaMemcpyAsync(c->U, c->aos, bytes, cudaMemcpyDeviceToDevice, c->stream));
     MMF_CUDA(cudaMemcpyAsync(c->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    c->indicator_restart();
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     if (chunk_out) *chunk_out = c->gp.chunk;
     if (warps_out) *warps_out = d2 ? c->gp.wpb : (c->gp.tile3d ? -1 : 0);

@@ -10,7 +10,7 @@
 
 namespace mmf {
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s, float *Q);
+                          unsigned char *flags, cudaStream_t s, float *Q, unsigned char *raw, IndicatorStep is);
 }
 
 using namespace mmf;
@@ -40,6 +40,9 @@ struct mmf_ctx {
     mmf_mlp *indicator = nullptr;       // learned indicator run at the start of every step
     float ind_threshold = 0.5f;
     float *ind_q = nullptr;             // the indicator's FP32 primitive planes (5 x plane)
+    int ind_period = 1;                 // the indicator runs every ind_period steps (1 or 2)
+    int *ind_tick = nullptr;            // device step counter of the period
+    unsigned char *ind_raw = nullptr;   // the network's flags before the dilation (period 2)
     // pipelined host round trip (mmf_advance_host): a copy stream, one event
     // per band and direction, pinned host words for the flag and the control block
     static constexpr int MAX_BANDS = 8;
@@ -86,6 +89,8 @@ struct mmf_ctx {
         oa.ctrl = ctrl; oa.stage = st;
         oa.cell0 = cell0;
         oa.cell1 = cell1;
+        // a step's stage-1 slopes advance the indicator's step counter
+        oa.tick = (op == O2_SLOPES && st == STAGE_1 && indicator && ind_period > 1) ? ind_tick : nullptr;
         ++launches;
         return (grid.arith == MMF_ARITH_FAST && st != STAGE_RHS) ? mmf::launch_o2_fast(op, st, g, sa, oa, W, on, w_zero)
                                                                 : mmf::launch_o2_exact(op, st, g, sa, oa, W, on);
@@ -97,8 +102,10 @@ struct mmf_ctx {
             // stage 1: slopes(U), R = RHS(U); stage 2: W1 = U + dt R / V, slopes(W1), R := W2;
             // stage 3: slopes(W2), U := 1/3 U + 2/3 (W2 + dt RHS(W2) / V)
             if (indicator) {
-                launches += 2;   // primitives, then features + MLP
-                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream, ind_q)) != cudaSuccess)
+                launches += ind_period > 1 ? 3 : 2;   // primitives, features + MLP (, dilation)
+                if ((e = mlp_indicator(indicator, gp, U, ind_threshold, nullptr, lim_flag, stream, ind_q,
+                                       ind_period > 1 ? ind_raw : nullptr, IndicatorStep{ind_period, ind_tick})) !=
+                    cudaSuccess)
                     return e;
             }
             if ((e = o2(O2_SLOPES, STAGE_1, U, nullptr, lim_active)) != cudaSuccess) return e;
@@ -113,7 +120,12 @@ struct mmf_ctx {
         if ((e = stage(STAGE_2, U, W)) != cudaSuccess) return e;
         return stage(STAGE_3, U, U);
     }
-    int launches_per_step() const { return grid.order == 2 ? (indicator ? 9 : 7) : 3; }
+    int launches_per_step() const { return grid.order == 2 ? (indicator ? (ind_period > 1 ? 10 : 9) : 7) : 3; }
+    // the next step runs the indicator (after a change of the state or of the time control)
+    void indicator_restart()
+    {
+        if (ind_tick) cudaMemsetAsync(ind_tick, 0, sizeof(int), stream);
+    }
 };
 
 

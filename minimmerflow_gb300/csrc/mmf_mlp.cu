@@ -50,7 +50,8 @@ static int mlp_pack(mmf_mlp *p)
 
 template <int DIM, int SRC>
 static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const float *Q, const __nv_bfloat16 *X, float thr,
-                                float *prob, unsigned char *flags, cudaStream_t s, BatchGeom bg = BatchGeom{nullptr, nullptr, 0})
+                                float *prob, unsigned char *flags, cudaStream_t s, BatchGeom bg = BatchGeom{nullptr, nullptr, 0},
+                                IndicatorStep is = IndicatorStep{1, nullptr})
 {
     const int smem = mlp_infer_smem<DIM>();
     cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel<DIM, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -64,44 +65,58 @@ static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const float *Q
     w.w1c = p->w1c;
     w.w2c = p->w2c;
     w.params = p->params;
-    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, Q, X, w, thr, prob, flags, p->err, bg, p->lim);
+    mlp_infer_kernel<DIM, SRC><<<blocks, 128, smem, s>>>(gp, Q, X, w, thr, prob, flags, p->err, bg, p->lim, is);
     return cudaPeekAtLastError();
 }
 
 // The primitive planes Q (5 x n FP32) of SoA FP64 planes U n apart.
-static cudaError_t launch_prims(long long n, const double *U, float *Q, cudaStream_t s)
+static cudaError_t launch_prims(long long n, const double *U, float *Q, cudaStream_t s, IndicatorStep is)
 {
     const long long b = (n + 255) / 256;
-    mlp_prims_kernel<<<(unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16), 256, 0, s>>>(n, U, Q);
+    mlp_prims_kernel<<<(unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16), 256, 0, s>>>(n, U, Q, is);
     return cudaPeekAtLastError();
 }
 
 // Features + MLP over a grid state (used by the solver context): the
 // primitive planes of U into Q (scratch of 5 x gp.plane floats), then the
-// fused kernel.
+// fused kernel.  With 'raw' (one byte per cell) the network's flags go there
+// and 'flags' receives them dilated by one cell.  'is' makes the launches of
+// the steps between two indicator runs do nothing.
 cudaError_t mlp_indicator(mmf_mlp *p, const GridParams &gp, const double *U, float thr, float *prob,
-                          unsigned char *flags, cudaStream_t s, float *Q)
+                          unsigned char *flags, cudaStream_t s, float *Q, unsigned char *raw, IndicatorStep is)
 {
     if (p->dim != gp.dim || !Q) return cudaErrorInvalidValue;
-    cudaError_t e = launch_prims(gp.plane, U, Q, s);
+    cudaError_t e = launch_prims(gp.plane, U, Q, s, is);
     if (e != cudaSuccess) return e;
-    return p->dim == 3 ? launch_infer<3, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, flags, s)
-                       : launch_infer<2, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, flags, s);
+    unsigned char *out = raw ? raw : flags;
+    e = p->dim == 3 ? launch_infer<3, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, out, s, BatchGeom{nullptr, nullptr, 0}, is)
+                    : launch_infer<2, MLP_SRC_GRID>(p, gp, Q, nullptr, thr, prob, out, s, BatchGeom{nullptr, nullptr, 0}, is);
+    if (e != cudaSuccess || !raw || !flags) return e;
+    const long long b = (gp.plane + 255) / 256;
+    const unsigned blocks = (unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
+    if (p->dim == 3) mlp_dilate_kernel<3><<<blocks, 256, 0, s>>>(gp, raw, flags, is);
+    else mlp_dilate_kernel<2><<<blocks, 256, 0, s>>>(gp, raw, flags, is);
+    return cudaPeekAtLastError();
 }
 
-// Indicator over a packed batch of 2D grids (total cells; Q: 5 x total floats).
+// Indicator over a packed batch of 2D grids (total cells; Q: 5 x total floats;
+// raw and is as for mlp_indicator).
 cudaError_t mlp_indicator_batch(mmf_mlp *p, const CaseDesc *cases, const long long *offsets, int ncases,
                                 long long total, const double *U, float thr, unsigned char *flags, cudaStream_t s,
-                                float *Q)
+                                float *Q, unsigned char *raw, IndicatorStep is)
 {
     if (p->dim != 2 || !Q) return cudaErrorInvalidValue;
     GridParams gp;
     memset(&gp, 0, sizeof(gp));
     gp.dim = 2;
     gp.plane = total;
-    cudaError_t e = launch_prims(total, U, Q, s);
+    cudaError_t e = launch_prims(total, U, Q, s, is);
     if (e != cudaSuccess) return e;
-    return launch_infer<2, MLP_SRC_BATCH>(p, gp, Q, nullptr, thr, nullptr, flags, s, BatchGeom{cases, offsets, ncases});
+    const BatchGeom bg{cases, offsets, ncases};
+    e = launch_infer<2, MLP_SRC_BATCH>(p, gp, Q, nullptr, thr, nullptr, raw ? raw : flags, s, bg, is);
+    if (e != cudaSuccess || !raw) return e;
+    mlp_dilate_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(bg, total, raw, flags, is);
+    return cudaPeekAtLastError();
 }
 
 cudaError_t mlp_features(int dim, const GridParams &gp, const double *U, void *X, cudaStream_t s)

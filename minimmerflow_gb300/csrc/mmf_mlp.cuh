@@ -157,8 +157,9 @@ __device__ __forceinline__ void prim_q_at(const float *Q, const GridParams &gp, 
 // SoA planes n apart: each cell converted once per indicator run, instead of
 // once per stencil (or strip) that contains it.
 __global__ void __launch_bounds__(256) mlp_prims_kernel(long long n, const double *__restrict__ U,
-                                                        float *__restrict__ Q)
+                                                        float *__restrict__ Q, IndicatorStep is)
 {
+    if (indicator_idle(is)) return;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         float q[5];
         prim_of(U, n, g, q);
@@ -198,13 +199,26 @@ __device__ __forceinline__ void cell_features_q(const float *Q, const GridParams
     int x, y, z;
     cell_coords(gp, g, x, y, z);
     if (DIM == 2) z = 0;
-    long long idx[NS];
+    // the neighbours' coordinates along each axis (wrapped or clamped as in
+    // stencil_index), then the stencil's 3^DIM indices as row offsets + x
+    const bool px = gp.bc_lo[0] == BC_PERIODIC, py = gp.bc_lo[1] == BC_PERIODIC, pz = gp.bc_lo[2] == BC_PERIODIC;
+    const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
+    int xs[3], ys[3], zs[3];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = DIM == 3 ? s / 9 - 1 : 0;
-        idx[s] = stencil_index(gp, x + dx, y + dy, z + dz);
+    for (int d = 0; d < 3; ++d) {
+        const int xx = x + d - 1, yy = y + d - 1, zz = z + d - 1;
+        xs[d] = xx < 0 ? (px ? nx - 1 : 0) : (xx >= nx ? (px ? 0 : nx - 1) : xx);
+        ys[d] = yy < 0 ? (py ? ny - 1 : 0) : (yy >= ny ? (py ? 0 : ny - 1) : yy);
+        zs[d] = DIM == 3 ? (zz < 0 ? (pz ? nz - 1 : 0) : (zz >= nz ? (pz ? 0 : nz - 1) : zz)) : 0;
     }
-    stencil_features<DIM>([&](int s, int v) { return __ldg(Q + v * gp.plane + idx[s]); }, put);
+    long long row[NS / 3];
+#pragma unroll
+    for (int r = 0; r < NS / 3; ++r)
+        row[r] = (long long)nx * ((long long)ys[r % 3] + (long long)ny * zs[DIM == 3 ? r / 3 : 1]);
+    const float *Qv[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Qv[v] = Q + v * gp.plane;
+    stencil_features<DIM>([&](int s, int v) { return __ldg(Qv[v] + row[s / 3] + xs[s % 3]); }, put);
 }
 
 // Normalised stencil differences of the primitives get(s, v) (FP32), one
@@ -337,8 +351,9 @@ template <int DIM, int SRC>
 __global__ void __launch_bounds__(128, MLP_CTAS_PER_SM) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
                                                            unsigned char *flags, int *err, BatchGeom bg,
-                                                           WaitLimits lim)
+                                                           WaitLimits lim, IndicatorStep is)
 {
+    if (indicator_idle(is)) return;   // uniform over the grid: before any barrier or allocation
     constexpr int KP = mlp_kpad(DIM);
     extern __shared__ __align__(1024) unsigned char dyn[];
     // the layer-1 operand X (128 x KP) and, once its MMA has completed, the
@@ -497,6 +512,57 @@ template <int DIM>
 constexpr int mlp_infer_smem()
 {
     return (mlp_operand_elems(DIM) + MLP_H * mlp_kpad(DIM) + MLP_H * MLP_H) * 2;
+}
+
+// Dilation of the indicator's flags by one cell: flags[g] = 1 where a cell of
+// g's 3^DIM neighbourhood (wrapped or clamped as in stencil_index) has raw = 1.
+template <int DIM>
+__global__ void __launch_bounds__(256) mlp_dilate_kernel(GridParams gp, const unsigned char *__restrict__ raw,
+                                                         unsigned char *__restrict__ flags, IndicatorStep is)
+{
+    if (indicator_idle(is)) return;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < gp.plane;
+         g += (long long)gridDim.x * blockDim.x) {
+        int x, y, z;
+        cell_coords(gp, g, x, y, z);
+        if (DIM == 2) z = 0;
+        unsigned m = 0;
+#pragma unroll
+        for (int dz = (DIM == 3 ? -1 : 0); dz <= (DIM == 3 ? 1 : 0); ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) m |= raw[stencil_index(gp, x + dx, y + dy, z + dz)];
+        flags[g] = m ? 1 : 0;
+    }
+}
+
+// The same over a packed batch of 2D grids, one thread per cell; each block
+// finds the case of its first cell once (a case has at least 32 x 32 cells,
+// so a block of 256 cells meets at most two).
+__global__ void __launch_bounds__(256) mlp_dilate_batch_kernel(BatchGeom bg, long long total,
+                                                               const unsigned char *__restrict__ raw,
+                                                               unsigned char *__restrict__ flags, IndicatorStep is)
+{
+    if (indicator_idle(is)) return;
+    __shared__ int s_case;
+    const long long g0 = blockIdx.x * 256LL;
+    if (threadIdx.x == 0) s_case = case_of(bg, g0);
+    __syncthreads();
+    const long long g = g0 + threadIdx.x;
+    if (g >= total) return;
+    int c = s_case;
+    while (c + 1 < bg.ncases && bg.offsets[c + 1] <= g) ++c;
+    const long long off = bg.offsets[c];
+    const GridParams &gp = bg.cases[c].gp;
+    int x, y, z;
+    cell_coords(gp, g - off, x, y, z);
+    unsigned m = 0;
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) m |= raw[off + stencil_index(gp, x + dx, y + dy, 0)];
+    flags[g] = m ? 1 : 0;
 }
 
 } // namespace mmf

@@ -44,7 +44,22 @@ struct O2Args {
     Ctrl *ctrl;
     int stage;               // 0 = residual-only call, 1..3 = RK stage
     long long cell0, cell1;  // slopes of grid cells [cell0, cell1) (a band of rows or planes)
+    int *tick = nullptr;     // the indicator's step counter, advanced by a step's stage-1 slopes (nullable)
 };
+
+// When the indicator runs every 'period' steps: the launches of a step whose
+// counter (advanced by each step's stage-1 slopes, reset to 0 when the state
+// or the time control changes) is not a multiple of the period do nothing,
+// and the flags of the last run stand, dilated by one cell.
+struct IndicatorStep {
+    int period;        // 1: every step
+    const int *tick;   // the step counter (period > 1)
+};
+
+__device__ __forceinline__ bool indicator_idle(const IndicatorStep &is)
+{
+    return is.period > 1 && (*is.tick % is.period) != 0;
+}
 
 // a*b <= 0 -> 0; else sign(a) min(2|a|, 2|b|, |central|)  (oracle orc_compute_polynomials)
 template <class A>
@@ -330,6 +345,8 @@ template <class A, int DIM>
 __global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
 {
     if (!o2_step_active(oa.ctrl, oa.stage)) return;
+    // no block of this launch reads the counter
+    if (oa.tick && blockIdx.x == 0 && threadIdx.x == 0) *oa.tick += 1;
     for (long long g = oa.cell0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < oa.cell1;
          g += (long long)gridDim.x * blockDim.x)
         slopes_cell<A, DIM>(gp, oa, g);

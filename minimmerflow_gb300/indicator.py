@@ -130,9 +130,12 @@ def generate_dataset(cases, snapshots=4, steps_between=6, samples=1_000_000, see
     return X, y
 
 
-def use_indicator(solver, mlp, threshold):
-    """Every following step of 'solver' starts with the indicator on U."""
+def use_indicator(solver, mlp, threshold, period=1):
+    """Every following step of 'solver' starts with the indicator on U, or
+    every second step with its flags dilated by one cell (period 2)."""
     capi.check(solver._lib.mmf_set_indicator(solver._ctx, mlp.handle if mlp is not None else None, threshold))
+    if mlp is not None:
+        capi.check(solver._lib.mmf_set_indicator_period(solver._ctx, period))
 
 
 def run_indicator(solver, mlp, threshold):

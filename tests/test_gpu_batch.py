@@ -109,6 +109,29 @@ def test_batch_order2_with_indicator_equals_single_contexts(mmf):
         assert np.array_equal(out[i], U), c.name
 
 
+def test_batch_indicator_every_second_step_equals_single_contexts(mmf):
+    """With the indicator run every second step (flags dilated by one cell),
+    the batch still gives every case the state of its own single-case run."""
+    from minimmerflow_gb300 import indicator
+    from minimmerflow_gb300.batch import BatchEuler
+    mlp = indicator.TroubledCellMLP(dim=2, seed=4)
+    p = mlp.params()
+    p[-1] = 0.0
+    mlp.set_params(p)
+    cases = [c for c in small_sweep(mmf, ncases=12, seed=22) if c.problem == mmf.problem.VORTEX_XY]
+    for c in cases:
+        c.cfl = 0.4
+    states = [c.initial_state() for c in cases]
+    with BatchEuler(cases, arith="fast", order=2) as b:
+        b.set_indicator(mlp, 0.5, period=2)
+        out = b.run(states, 7)
+    for i, (c, U0) in enumerate(zip(cases, states)):
+        with c.solver(arith="fast", order=2) as s:
+            indicator.use_indicator(s, mlp, 0.5, period=2)
+            U, t, n = s.run(U0, c.cfl, max_steps=7)
+        assert np.array_equal(out[i], U), c.name
+
+
 def test_full_sweep_every_case_equals_its_own_context(mmf):
     """The benchmark's sweep itself (512 cases, seed 20261203, sides 32..512):
     after 10 steps in one batch, every case holds exactly the state of its own
