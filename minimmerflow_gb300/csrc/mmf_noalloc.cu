@@ -136,10 +136,12 @@ extern "C" int mmf_compute_rhs_noalloc(const mmf_grid *grid, const double *d_con
     if (grid->arith != MMF_ARITH_REFERENCE)
         return set_last_error(MMF_ERR_UNSUPPORTED, "only the reference arithmetic is supported");
     long long n = 1;
-    for (int d = 0; d < grid->dim; ++d) n *= grid->n[d];
-    if (n > kMaxCells)
-        return set_last_error(MMF_ERR_ARG, "mmf_compute_rhs_noalloc: the mesh has more cells than "
-                                           "MMF_NOALLOC_MAX_CELLS (65536)");
+    for (int d = 0; d < grid->dim; ++d) {
+        n *= grid->n[d];   // n <= 65536 before, n[d] < 2^31: no overflow
+        if (n > kMaxCells)
+            return set_last_error(MMF_ERR_ARG, "mmf_compute_rhs_noalloc: the mesh has more cells than "
+                                               "MMF_NOALLOC_MAX_CELLS (65536)");
+    }
     double *scratch = nullptr;
     rc = scratch_of_current_device(&scratch);
     if (rc) return rc;

@@ -63,6 +63,10 @@ def test_noalloc_rejects_meshes_above_the_maximum(mmf):
     rc = lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None)
     assert rc == mmf.capi.MMF_ERR_ARG
     assert b"65536" in lib.mmf_last_error()
+    g = _grid(mmf, 2**31 - 1)   # extents whose product overflows 64 bits
+    g.dim, g.n[2] = 3, 2**31 - 1
+    assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_ARG
+    assert b"65536" in lib.mmf_last_error()
     g = _grid(mmf, 16)
     g.arith = mmf.capi.ARITH_FAST
     assert lib.mmf_compute_rhs_noalloc(C.byref(g), buf, buf, buf, None, None) == mmf.capi.MMF_ERR_UNSUPPORTED
