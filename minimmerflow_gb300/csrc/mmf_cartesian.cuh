@@ -519,10 +519,10 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
 // 256-cell grid lines exactly.  The records the tile's faces need from the
 // four neighbouring lines (the column left and right of the tile, the row
 // below and above it) are evaluated once per plane by three warps in one
-// extra pass each (x or y part only), and the faces on the tile's left and
-// bottom edges by two more warps; every other face is evaluated once, by the
-// cell on its low side: x faces move between lanes by shuffles, y faces go
-// through shared memory, z faces stay in registers along the march.
+// extra pass each (x or y part only), and the faces on the tile's left,
+// right and bottom edges by two more warps; every other face is evaluated
+// once, by the cell on its low side: x faces move between lanes by shuffles,
+// y faces go through shared memory, z faces stay in registers along the march.
 //
 // Two barriers per plane: (A) the plane's records are in shared memory,
 // (B) its faces are.  The next plane's records and halo records are written
@@ -544,8 +544,10 @@ struct SmemTile {
     double bc[NV][32], bf[NV][32], blam[32];                        // bottom halo row
     double xc[2][NV][TILE_Y], xf[2][NV][TILE_Y], xlam[2][TILE_Y];    // left [0] / right [1] halo column
     double c0[NV][TILE_Y], f0[NV][TILE_Y], lam0[TILE_Y];            // column 0 of the tile (x side)
+    double c31[NV][TILE_Y], f31[NV][TILE_Y], lam31[TILE_Y];         // column 31 of the tile (x side)
     double Fy[TILE_Y][NV][32];       // y face above row w
     double Fl[NV][TILE_Y];           // x face on the tile's left edge, row w
+    double Fr[NV][TILE_Y];           // x face on the tile's right edge, row w
     double Fb[NV][32];               // y face on the tile's bottom edge, column l
 };
 
@@ -578,7 +580,7 @@ __device__ __forceinline__ void tile_halo_records(const StageArgs &sa, const Gri
     }
 }
 
-// This row's y side, and column 0's x side, of record r.
+// This row's y side, and the x side of columns 0 and 31, of record r.
 template <int NV>
 __device__ __forceinline__ void tile_publish(SmemTile<NV> &sm, const CellRecV<3, NV> &r, int w, int l)
 {
@@ -589,6 +591,10 @@ __device__ __forceinline__ void tile_publish(SmemTile<NV> &sm, const CellRecV<3,
 #pragma unroll
         for (int k = 0; k < NV; ++k) { sm.c0[k][w] = r.c[k]; sm.f0[k][w] = r.f[0][k]; }
         sm.lam0[w] = r.lam[0];
+    } else if (l == 31) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { sm.c31[k][w] = r.c[k]; sm.f31[k][w] = r.f[0][k]; }
+        sm.lam31[w] = r.lam[0];
     }
 }
 
@@ -632,19 +638,15 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
     tile_publish<NV>(sm, cur, w, l);
     for (int z = z0; z < z1; ++z) {
         __syncthreads();   // (A) records of plane z
-        // x face on the right: the next lane, or the right halo column
+        // x face on the right: the next lane (lane 31's, on the tile's right
+        // edge, comes from the edge pass; its value here is replaced)
         {
             double cR[NV], fR[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) { cR[k] = shfl_down(cur.c[k], 1); fR[k] = shfl_down(cur.f[0][k], 1); }
-            double lamR = shfl_down(cur.lam[0], 1);
-            if (l == 31) {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) { cR[k] = sm.xc[1][k][w]; fR[k] = sm.xf[1][k][w]; }
-                lamR = sm.xlam[1][w];
-            }
+            const double lamR = shfl_down(cur.lam[0], 1);
             const double lx = A::face(cur.c, cur.f[0], cur.lam[0], cR, fR, lamR, Fxr);
-            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lx);
+            if (STAGE <= STAGE_1 && out && l < 31) lmax = max_nonneg(lmax, lx);
         }
         // y face above: the next row, or the top halo row
         {
@@ -656,16 +658,26 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
 #pragma unroll
             for (int k = 0; k < NV; ++k) sm.Fy[w][k][l] = Fyt[k];
         }
-        // faces on the tile's left edge (lanes 0..15: rows) and bottom edge (lanes: columns)
+        // faces on the tile's left edge (lanes 0..15: rows), right edge (lanes
+        // 16..31: rows) and bottom edge (lanes: columns)
         if (w == TW_LEFTF) {
             const int r = l & 15;
+            const bool right = l >= 16;
             double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                cL[k] = sm.xc[0][k][r]; fL[k] = sm.xf[0][k][r]; cR[k] = sm.c0[k][r]; fR[k] = sm.f0[k][r];
+                cL[k] = right ? sm.c31[k][r] : sm.xc[0][k][r];
+                fL[k] = right ? sm.f31[k][r] : sm.xf[0][k][r];
+                cR[k] = right ? sm.xc[1][k][r] : sm.c0[k][r];
+                fR[k] = right ? sm.xf[1][k][r] : sm.f0[k][r];
             }
-            const double le = A::face(cL, fL, sm.xlam[0][r], cR, fR, sm.lam0[r], F);
-            if (l < 16) {
+            const double le = A::face(cL, fL, right ? sm.lam31[r] : sm.xlam[0][r], cR, fR,
+                                      right ? sm.xlam[1][r] : sm.lam0[r], F);
+            if (right) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.Fr[k][r] = F[k];
+                if (STAGE <= STAGE_1 && x0 + TILE_X - 1 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
+            } else {
 #pragma unroll
                 for (int k = 0; k < NV; ++k) sm.Fl[k][r] = F[k];
                 if (STAGE <= STAGE_1 && x0 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
@@ -688,6 +700,7 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
         for (int k = 0; k < NV; ++k) {
             const double fl = shfl_up(Fxr[k], 1);
             Fxl[k] = (l == 0) ? sm.Fl[k][w] : fl;
+            Fxr[k] = (l == 31) ? sm.Fr[k][w] : Fxr[k];
             Fyb[k] = (w == 0) ? sm.Fb[k][l] : sm.Fy[wb][k][l];
         }
         accumulate_pair<A, true>(acc, Fxl, Fxr, gp.area, perx && x == nx - 1);
