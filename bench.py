@@ -547,6 +547,119 @@ def run_equal_error(args, local, t_end=2.0, plain_n=1024):
     return out
 
 
+def run_batched_equal_error(args, local, t_end=2.0, ncases=256, per_case=False):
+    """Time to solution at equal accuracy for a batch: the vortex half of the
+    seeded sweep (ncases isentropic vortices, beta ~ U[1,8], mesh side
+    U{32..512}, periodic [-5,5]^2) to t = 2.
+    - plain: the plain FP64 path (order 1, the reference's method, CFL 0.5)
+      on every case's own mesh, as one batch;
+    - learned: the batched order 2 with the learned indicator (CFL 0.4), each
+      case on the coarsest mesh of a ladder whose L1 density error against
+      the exact solution (src/main.cpp:550-561) is at most 1.01 times that
+      case's plain error (the plain side itself when no coarser one is);
+    - limited: the batched order 2 with every cell limited on the same meshes.
+    Each timed run is one advance of exactly the steps that take every case
+    to t = 2 (counted by an untimed run), after the shape is tuned, on the
+    host clock around the advance and its synchronisation."""
+    from minimmerflow_gb300.batch import BatchEuler
+    from minimmerflow_gb300 import train_indicator
+    import minimmerflow_gb300 as mmf
+
+    mlp, thr = train_indicator.load(2, device=local)
+    if mlp is None:
+        mlp, _, thr = train_indicator.train(2, samples=1_000_000, epochs=8, log=None)
+    sweep = [c for c in mmf.problem.batched_sweep(ncases=2 * ncases, seed=args.seed)
+             if c.problem == mmf.problem.VORTEX_XY][:ncases]
+    betas = [c.prm.vortex_beta for c in sweep]
+    sides = [int(c.n[0]) for c in sweep]
+
+    def make(idx, n_of, cfl):
+        cs = []
+        for i, n in zip(idx, n_of):
+            b = betas[i]
+            c = mmf.problem.vortex(2, n, steps=-1, beta=b, cfl=cfl)
+            c.t_end = t_end
+            cs.append(c)
+        return cs
+
+    def solve(cs, order, mode, timed):
+        with BatchEuler(cs, arith=args.arith, device=local, order=order) as b:
+            if mode == "learned":
+                b.set_indicator(mlp, thr)
+            U0 = b.pack([c.initial_state() for c in cs])
+            te = np.full(len(cs), t_end)
+            b.upload(U0)
+            b.time_setup(t_end=te)
+            if timed:
+                b.autotune(trial_steps=2)
+                b.upload(U0)
+                b.time_setup(t_end=te)
+            steps = 0
+            while True:   # untimed: the steps that take every case to t_end
+                b.advance_async(64)
+                b.synchronize()
+                steps += 64
+                info = [b.case_info(i) for i in range(len(cs))]
+                if all(t >= t_end for t, _, _ in info):
+                    break
+            nsteps = max(s for _, s, _ in info)
+            secs = None
+            if timed:
+                b.upload(U0)
+                b.time_setup(t_end=te)
+                b.synchronize()
+                t0 = time.perf_counter()
+                b.advance_async(nsteps)
+                b.synchronize()
+                secs = time.perf_counter() - t0
+                info = [b.case_info(i) for i in range(len(cs))]
+                assert all(t == t_end and st == 0 for t, _, st in info)
+            U = b.unpack(b.download())
+            errs = [c.l1_density_error(u, t_end) for c, u in zip(cs, U)]
+            updates = int(sum(c.ncells * s for c, (_, s, _) in zip(cs, info)))
+        return errs, secs, updates, nsteps
+
+    every = range(len(sides))
+    plain_err, plain_s, plain_upd, plain_steps = solve(make(every, sides, 0.5), 1, "plain", True)
+    ladder = (8, 12, 16, 20, 24, 28, 32, 40, 48, 56, 64, 80, 96, 112, 128, 160, 192, 256, 320, 384, 448, 512)
+    chosen = [None] * len(sides)
+    for L in ladder:
+        todo = [i for i in range(len(sides)) if chosen[i] is None]
+        if not todo:
+            break
+        n_try = [min(L, sides[i]) for i in todo]
+        errs, _, _, _ = solve(make(todo, n_try, 0.4), 2, "learned", False)
+        for i, n, e in zip(todo, n_try, errs):
+            if e <= 1.01 * plain_err[i] or n == sides[i]:
+                chosen[i] = n
+    learned_err, learned_s, learned_upd, learned_steps = solve(make(every, chosen, 0.4), 2, "learned", True)
+    limited_err, limited_s, limited_upd, _ = solve(make(every, chosen, 0.4), 2, "limited", True)
+    mlp.close()
+    ratio = np.array(learned_err) / np.array(plain_err)
+    out = {
+        "cases": len(sides), "t_end": t_end,
+        "workload": "the vortex half of the seeded batched sweep (seed %d): isentropic vortices beta~U[1,8], "
+                    "side U{32..512}, periodic [-5,5]^2, to t = %g, FP64" % (args.seed, t_end),
+        "plain_order1": {"seconds": plain_s, "cell_updates": plain_upd, "steps_max": plain_steps,
+                         "cells": int(sum(s * s for s in sides)), "l1_density_error_sum": float(sum(plain_err))},
+        "learned_order2": {"seconds": learned_s, "cell_updates": learned_upd, "steps_max": learned_steps,
+                           "cells": int(sum(n * n for n in chosen)), "threshold": thr,
+                           "l1_density_error_sum": float(sum(learned_err)),
+                           "error_ratio_over_plain": {"max": float(ratio.max()), "mean": float(ratio.mean())},
+                           "side_over_plain_side": {"median": float(np.median(np.array(chosen) / np.array(sides))),
+                                                    "max": float(np.max(np.array(chosen) / np.array(sides)))}},
+        "limited_order2_same_meshes": {"seconds": limited_s, "cell_updates": limited_upd,
+                                       "l1_density_error_sum": float(sum(limited_err))},
+        "time_ratio_plain_over_learned": plain_s / learned_s,
+        "plain_equivalent_cell_updates_per_s": plain_upd / learned_s,
+        "time_ratio_limited_over_learned": limited_s / learned_s,
+    }
+    if per_case:
+        out["per_case"] = {"beta": betas, "side": sides, "learned_side": chosen, "plain_error": plain_err,
+                           "learned_error": learned_err, "limited_error": limited_err}
+    return out
+
+
 def run_dropin(args, local, steps):
     """The reference loop (src/main.cpp:377-506) through the minimal drop-in
     binding: per stage one mmf_compute_rhs call on host buffers (upload of the
@@ -1199,6 +1312,7 @@ def main():
         guarded("sod3d_learned", learned3d)
         guarded("dropin_binding", lambda: run_dropin(args, local, max(3, min(args.steps, 5))))
         guarded("equal_error_vortex", lambda: run_equal_error(args, local))
+        guarded("batched_equal_error", lambda: run_batched_equal_error(args, local))
     if not args.no_cpu and args.workload == "sod2d":
         line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds, 1)
     print(json.dumps(line))
