@@ -448,6 +448,64 @@ __device__ __forceinline__ void load_sides(const GridParams &gp, const double *s
         for (int s = 0; s < 2; ++s) side_record<A, DIM>(gs, d, sr.r[d][s], nullptr);
 }
 
+// What load_sides reads for a cell, before any face-side record is evaluated:
+// the stage state and slopes of an interior cell, or the ghost face state of
+// a ghost position (which every side of the ghost shows).  The 3D kernel
+// keeps this (20 doubles) for the next plane instead of its six records
+// (66), and evaluates each record where it is used.
+template <class A, int DIM>
+struct SideSrc {
+    double uc[A::NVAR];
+    double sg[DIM][A::NVAR];
+    bool ghost;
+};
+
+template <class A, int DIM>
+__device__ __forceinline__ void load_src(const GridParams &gp, const double *state, const double *S, int x, int y,
+                                         int z, SideSrc<A, DIM> &src)
+{
+    constexpr int NV = A::NVAR;
+    int gx, gy, gz = 0;
+    const int ix = resolve_index(x, gp.n[0], gp.bc_lo[0] == BC_PERIODIC, gx);
+    const int iy = resolve_index(y, gp.n[1], gp.bc_lo[1] == BC_PERIODIC, gy);
+    const int iz = (DIM == 3) ? resolve_index(z, gp.n[2], gp.bc_lo[2] == BC_PERIODIC, gz) : 0;
+    const long long n = gp.plane;
+    const long long g = (long long)ix + (long long)gp.n[0] * ((long long)iy + (long long)gp.n[1] * iz);
+    load_plain<A>(state, n, g, src.uc);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) src.sg[d][k] = __ldg(S + (long long)(d * NV + k) * n + g);
+    const int gh[3] = {gx, gy, gz};
+    int gdir = -1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) if (gh[d] != 0 && gdir < 0) gdir = d;
+    src.ghost = gdir >= 0;
+    if (gdir >= 0) {   // as load_sides: the ghost of the interior cell's face state
+        double gs[NV];
+        const double off = gh[gdir] > 0 ? 0.5 : -0.5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) gs[k] = face_value<A>(src.uc[k], off, src.sg[gdir][k]);
+        ghost_in_place<A, true>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], gdir, gh[gdir], gs, gp.dir_cons);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) src.uc[k] = gs[k];
+    }
+}
+
+// Record of side (d, s) of src: the record load_sides gives as r[d][s]
+// (status only for interior cells' + sides, as there).
+template <class A, int DIM>
+__device__ __forceinline__ void side_of(const SideSrc<A, DIM> &src, int d, int s, CellRecV<1, A::NVAR> &out,
+                                        unsigned *status)
+{
+    constexpr int NV = A::NVAR;
+    double fs[NV];
+    const double off = s ? 0.5 : -0.5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) fs[k] = src.ghost ? src.uc[k] : face_value<A>(src.uc[k], off, src.sg[d][k]);
+    side_record<A, DIM>(fs, d, out, (s == 1 && !src.ghost) ? status : nullptr);
+}
+
 template <class A>
 __device__ __forceinline__ double side_face(const CellRecV<1, A::NVAR> &L, const CellRecV<1, A::NVAR> &R, double *F)
 {
@@ -565,9 +623,15 @@ struct Smem3DO2 {
     double F[BY][NV][32];
 };
 
+// Registers: the next plane is kept as its state and slopes (SideSrc), and
+// each face-side record is evaluated where its face is, so that the kernel
+// fits MinBlocks blocks per SM.
+template <class A> struct O2Stage3DMinBlocks { static constexpr int value = 1; };
+template <> struct O2Stage3DMinBlocks<FastArithT<5>> { static constexpr int value = 2; };
+
 template <class A, int STAGE, int BY>
-__global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, StageArgs sa, const double *state,
-                                                             const double *S)
+__global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A>::value)
+    stage3d_o2_kernel(GridParams gp, StageArgs sa, const double *state, const double *S)
 {
     constexpr int NV = A::NVAR;
     __shared__ Smem3DO2<BY, NV> sm;
@@ -599,12 +663,18 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
     unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
     double lmax = 0.0;
 
-    SideRec<A, 3> cur, abv;
+    SideSrc<A, 3> cur;
     double Fzlo[NV], Fzhi[NV], Fa[NV], Fb[NV], acc[NV];
     if (!halo_lo && !halo_hi && !idle) {
-        load_sides<A, 3>(gp, state, S, x, y, z0 - 1, abv, nullptr);
-        load_sides<A, 3>(gp, state, S, x, y, z0, cur, st);
-        const double l = side_face<A>(abv.r[2][1], cur.r[2][0], Fzlo);
+        CellRecV<1, NV> below, zm;
+        {
+            SideSrc<A, 3> bl;
+            load_src<A, 3>(gp, state, S, x, y, z0 - 1, bl);
+            side_of<A, 3>(bl, 2, 1, below, nullptr);
+        }
+        load_src<A, 3>(gp, state, S, x, y, z0, cur);
+        side_of<A, 3>(cur, 2, 0, zm, nullptr);
+        const double l = side_face<A>(below, zm, Fzlo);
         if (out) lmax = max_nonneg(lmax, l);
     }
     for (int z = z0; z < z1; ++z) {
@@ -615,10 +685,13 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
             continue;
         }
         if (halo_lo || halo_hi) {
-            SideRec<A, 3> h;
-            load_sides<A, 3>(gp, state, S, x, y, z, h, nullptr);
             // the face side this halo row shows to the block: +y for the row below, -y above
-            const CellRecV<1, NV> &hr = halo_lo ? h.r[1][1] : h.r[1][0];
+            CellRecV<1, NV> hr;
+            {
+                SideSrc<A, 3> h;
+                load_src<A, 3>(gp, state, S, x, y, z, h);
+                side_of<A, 3>(h, 1, halo_lo ? 1 : 0, hr, nullptr);
+            }
 #pragma unroll
             for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = hr.c[k]; sm.f[w][k][lane] = hr.f[0][k]; }
             sm.lam[w][lane] = hr.lam[0];
@@ -637,20 +710,30 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
             __syncthreads();
             continue;
         }
-        const double lx = xfaces_o2<A>(cur.r[0][1], cur.r[0][0], Fa, Fb);
-        if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = max_nonneg(lmax, lx);
+        {
+            CellRecV<1, NV> xp, xm;
+            side_of<A, 3>(cur, 0, 1, xp, st);
+            side_of<A, 3>(cur, 0, 0, xm, nullptr);
+            const double lx = xfaces_o2<A>(xp, xm, Fa, Fb);
+            if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = max_nonneg(lmax, lx);
+        }
         accumulate_pair<A, true>(acc, Fa, Fb, gp.area, perx && x == nx - 1);
         // y faces: rows publish their +y side, each row evaluates the face below it
+        {
+            CellRecV<1, NV> yp;
+            side_of<A, 3>(cur, 1, 1, yp, st);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = cur.r[1][1].c[k]; sm.f[w][k][lane] = cur.r[1][1].f[0][k]; }
-        sm.lam[w][lane] = cur.r[1][1].lam[0];
+            for (int k = 0; k < NV; ++k) { sm.c[w][k][lane] = yp.c[k]; sm.f[w][k][lane] = yp.f[0][k]; }
+            sm.lam[w][lane] = yp.lam[0];
+        }
         __syncthreads();
         {
-            CellRecV<1, NV> L;
+            CellRecV<1, NV> L, ym;
+            side_of<A, 3>(cur, 1, 0, ym, nullptr);
 #pragma unroll
             for (int k = 0; k < NV; ++k) { L.c[k] = sm.c[w - 1][k][lane]; L.f[0][k] = sm.f[w - 1][k][lane]; }
             L.lam[0] = sm.lam[w - 1][lane];
-            const double ly = side_face<A>(L, cur.r[1][0], Fa);
+            const double ly = side_face<A>(L, ym, Fa);
 #pragma unroll
             for (int k = 0; k < NV; ++k) sm.F[w][k][lane] = Fa[k];
             if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
@@ -659,16 +742,21 @@ __global__ void __launch_bounds__(BY * 32) stage3d_o2_kernel(GridParams gp, Stag
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fb[k] = sm.F[w + 1][k][lane];
         accumulate_pair<A, false>(acc, Fa, Fb, gp.area, pery && y == ny - 1);
-        load_sides<A, 3>(gp, state, S, x, y, z + 1, abv, (z + 1 < z1) ? st : nullptr);
-        const double lz = side_face<A>(cur.r[2][1], abv.r[2][0], Fzhi);
-        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+        // z face above: this plane's +z side, the next plane's -z side
+        {
+            CellRecV<1, NV> zp, zm;
+            side_of<A, 3>(cur, 2, 1, zp, st);
+            load_src<A, 3>(gp, state, S, x, y, z + 1, cur);
+            side_of<A, 3>(cur, 2, 0, zm, nullptr);
+            const double lz = side_face<A>(zp, zm, Fzhi);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+        }
         if (out) {
             accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
             store_output_o2<A, STAGE>(sa, gp, sc, state,
                                       (long long)x + (long long)nx * ((long long)y + (long long)ny * z), acc);
         }
         __syncthreads();
-        cur = abv;
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
     }
