@@ -91,13 +91,30 @@ struct RowPacker {
 };
 
 // GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))),
-// written as x sigma(z) with z = 2 sqrt(2/pi) (x + 0.044715 x^3): one
-// exponential and one reciprocal per value (the network applies 128 per cell).
+// written as x sigma(z) with z = 2 sqrt(2/pi) (x + 0.044715 x^3) and
+// sigma(z) = 1 / (1 + 2^(-z log2 e)): the exponent -z log2 e as one
+// polynomial in x with folded constants, then the hardware base-2
+// exponential and reciprocal approximations (the network applies 128 per
+// cell, so this is most of the inference's arithmetic).
 constexpr float GELU_C = 1.5957691216057308f;   // 2 sqrt(2 / pi)
+constexpr float GELU_E1 = -1.5957691216057308f * 1.4426950408889634f;   // -GELU_C log2 e
+constexpr float GELU_E3 = GELU_E1 * 0.044715f;
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float gelu(float x)
 {
-    const float z = GELU_C * fmaf(0.044715f * x, x * x, x);
-    return __fdividef(x, 1.0f + __expf(-z));
+    const float t = x * fmaf(GELU_E3, x * x, GELU_E1);   // -z log2 e
+    return x * rcp_approx(1.0f + ex2_approx(t));
 }
 __device__ __forceinline__ float gelu_grad(float x)
 {
