@@ -625,12 +625,12 @@ struct Smem3DO2 {
 
 // Registers: the next plane is kept as its state and slopes (SideSrc), and
 // each face-side record is evaluated where its face is, so that the kernel
-// fits MinBlocks blocks per SM.
-template <class A> struct O2Stage3DMinBlocks { static constexpr int value = 1; };
-template <> struct O2Stage3DMinBlocks<FastArithT<5>> { static constexpr int value = 2; };
+// fits 128 registers: two blocks of 8 warps (one of 16) per SM.
+template <class A, int BY> struct O2Stage3DMinBlocks { static constexpr int value = 1; };
+template <int BY> struct O2Stage3DMinBlocks<FastArithT<5>, BY> { static constexpr int value = BY <= 8 ? 2 : 1; };
 
 template <class A, int STAGE, int BY>
-__global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A>::value)
+__global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A, BY>::value)
     stage3d_o2_kernel(GridParams gp, StageArgs sa, const double *state, const double *S)
 {
     constexpr int NV = A::NVAR;
