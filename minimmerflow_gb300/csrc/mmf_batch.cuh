@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(128) form_w1_batch_kernel(const CaseDesc *__re
 
 // Minimum resident blocks per SM the order-2 batch march is compiled for:
 // the four-field fast variant (2D states with zero z-momentum, the batched
-// sweep's) gets the 128 registers the single-grid march reaches on its own,
-// so that four persistent blocks of four warps fit on an SM.
+// sweep's) gets 128 registers, so that four persistent blocks of four warps
+// fit on an SM (at five, 102 registers, it spills 200-260 B).
 template <class A> struct O2BatchMinBlocks { static constexpr int value = 1; };
 template <> struct O2BatchMinBlocks<FastArithT<4>> { static constexpr int value = 4; };
 

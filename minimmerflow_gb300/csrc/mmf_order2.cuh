@@ -381,10 +381,6 @@ __global__ void __launch_bounds__(256) form_w1_kernel(GridParams gp, StageArgs s
 // interior U + s sigma_d / 2 (reconstruction eval, oracle eval_side); a ghost
 // across the border of direction d shows the ghost of the neighbouring
 // interior cell's face state (euler.cpp:224-225).
-template <class A, int DIM>
-struct SideRec {
-    CellRecV<1, A::NVAR> r[DIM][2];   // [direction][side: 0 = -e_d, 1 = +e_d]
-};
 
 // Record for one face side: record() on a face state, keeping direction d only.
 template <class A, int DIM>
@@ -399,60 +395,11 @@ __device__ __forceinline__ void side_record(const double *c, int d, CellRecV<1, 
     out.lam[0] = full.lam[d];
 }
 
-// Face-side records of the cell at (x, y, z), which may be a ghost position.
-template <class A, int DIM>
-__device__ __forceinline__ void load_sides(const GridParams &gp, const double *state, const double *S, int x, int y,
-                                           int z, SideRec<A, DIM> &sr, unsigned *status)
-{
-    constexpr int NV = A::NVAR;
-    int gx, gy, gz = 0;
-    const int ix = resolve_index(x, gp.n[0], gp.bc_lo[0] == BC_PERIODIC, gx);
-    const int iy = resolve_index(y, gp.n[1], gp.bc_lo[1] == BC_PERIODIC, gy);
-    const int iz = (DIM == 3) ? resolve_index(z, gp.n[2], gp.bc_lo[2] == BC_PERIODIC, gz) : 0;
-    const long long n = gp.plane;
-    const long long g = (long long)ix + (long long)gp.n[0] * ((long long)iy + (long long)gp.n[1] * iz);
-    double uc[NV], sg[DIM][NV];
-    load_plain<A>(state, n, g, uc);
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sg[d][k] = __ldg(S + (long long)(d * NV + k) * n + g);
-    const int gh[3] = {gx, gy, gz};
-    int gdir = -1;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) if (gh[d] != 0 && gdir < 0) gdir = d;
-    if (gdir < 0) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                double fs[NV];
-                const double off = s ? 0.5 : -0.5;
-#pragma unroll
-                for (int k = 0; k < NV; ++k) fs[k] = face_value<A>(uc[k], off, sg[d][k]);
-                side_record<A, DIM>(fs, d, sr.r[d][s], s == 1 ? status : nullptr);
-            }
-        return;
-    }
-    // ghost across the border of direction gdir on side gh[gdir]: the face it
-    // shares with the interior cell is on its side -gh[gdir]; the interior
-    // face state is on the interior cell's side gh[gdir]
-    double gs[NV];
-    const double off = gh[gdir] > 0 ? 0.5 : -0.5;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) gs[k] = face_value<A>(uc[k], off, sg[gdir][k]);
-    ghost_in_place<A, true>(gh[gdir] < 0 ? gp.bc_lo[gdir] : gp.bc_hi[gdir], gdir, gh[gdir], gs, gp.dir_cons);
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-        for (int s = 0; s < 2; ++s) side_record<A, DIM>(gs, d, sr.r[d][s], nullptr);
-}
-
-// What load_sides reads for a cell, before any face-side record is evaluated:
-// the stage state and slopes of an interior cell, or the ghost face state of
-// a ghost position (which every side of the ghost shows).  The 3D kernel
-// keeps this (20 doubles) for the next plane instead of its six records
-// (66), and evaluates each record where it is used.
+// What a cell's face-side records are made from: the stage state and slopes
+// of an interior cell, or the ghost face state of a ghost position (which
+// every side of the ghost shows).  The marches keep this for the next row or
+// plane (12 doubles in 2D, 20 in 3D) instead of its 4 or 6 records (36, 66)
+// and evaluate each record where its face is.
 template <class A, int DIM>
 struct SideSrc {
     double uc[A::NVAR];
@@ -460,6 +407,7 @@ struct SideSrc {
     bool ghost;
 };
 
+// SideSrc of the cell at (x, y, z), which may be a ghost position.
 template <class A, int DIM>
 __device__ __forceinline__ void load_src(const GridParams &gp, const double *state, const double *S, int x, int y,
                                          int z, SideSrc<A, DIM> &src)
@@ -481,7 +429,10 @@ __device__ __forceinline__ void load_src(const GridParams &gp, const double *sta
 #pragma unroll
     for (int d = 0; d < DIM; ++d) if (gh[d] != 0 && gdir < 0) gdir = d;
     src.ghost = gdir >= 0;
-    if (gdir >= 0) {   // as load_sides: the ghost of the interior cell's face state
+    if (gdir >= 0) {
+        // ghost across the border of direction gdir on side gh[gdir]: the face
+        // it shares with the interior cell is on its side -gh[gdir]; the
+        // interior face state is on the interior cell's side gh[gdir]
         double gs[NV];
         const double off = gh[gdir] > 0 ? 0.5 : -0.5;
 #pragma unroll
@@ -492,8 +443,8 @@ __device__ __forceinline__ void load_src(const GridParams &gp, const double *sta
     }
 }
 
-// Record of side (d, s) of src: the record load_sides gives as r[d][s]
-// (status only for interior cells' + sides, as there).
+// Record of side (d, s: 0 = -e_d, 1 = +e_d) of src.  The state checks
+// (status) are taken on the + sides of interior cells.
 template <class A, int DIM>
 __device__ __forceinline__ void side_of(const SideSrc<A, DIM> &src, int d, int s, CellRecV<1, A::NVAR> &out,
                                         unsigned *status)
@@ -554,7 +505,10 @@ __device__ __forceinline__ void store_output_o2(const StageArgs &sa, const GridP
 }
 
 // ---------------------------------------------------------------- 2D, order 2
-// One warp's work item (as march2d, with face-side records).
+// One warp's work item (as march2d, with face-side records).  The next row
+// is kept as its state and slopes (SideSrc) and each face-side record is
+// evaluated where its face is: the +x and -x records for the x faces, this
+// row's +y record and the next row's -y record for the y face.
 template <class A, int STAGE>
 __device__ __forceinline__ void march2d_o2(const GridParams &gp, const StageArgs &sa, const double *state,
                                            const double *S, const StepScalars &sc, int seg, int chunk, double &lmax,
@@ -571,29 +525,46 @@ __device__ __forceinline__ void march2d_o2(const GridParams &gp, const StageArgs
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC;
     unsigned *st = (STAGE == STAGE_1 && out_col) ? &status : nullptr;
 
-    SideRec<A, 2> cur, abv;
+    SideSrc<A, 2> cur;
     double Fylo[NV], Fyhi[NV], Fxlo[NV], Fxhi[NV], acc[NV];
-    load_sides<A, 2>(gp, state, S, x, y0 - 1, 0, abv, nullptr);
-    load_sides<A, 2>(gp, state, S, x, y0, 0, cur, st);
     {
-        const double l = side_face<A>(abv.r[1][1], cur.r[1][0], Fylo);
+        CellRecV<1, NV> below, ym;
+        {
+            SideSrc<A, 2> bl;
+            load_src<A, 2>(gp, state, S, x, y0 - 1, 0, bl);
+            side_of<A, 2>(bl, 1, 1, below, nullptr);
+        }
+        load_src<A, 2>(gp, state, S, x, y0, 0, cur);
+        side_of<A, 2>(cur, 1, 0, ym, nullptr);
+        const double l = side_face<A>(below, ym, Fylo);
         if (out_col) lmax = max_nonneg(lmax, l);
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) Fyhi[k] = 0.0;
 #pragma unroll 4
     for (int y = y0; y < y1; ++y) {
-        const double lx = xfaces_o2<A>(cur.r[0][1], cur.r[0][0], Fxlo, Fxhi);
-        if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
+        {
+            CellRecV<1, NV> xp, xm;
+            side_of<A, 2>(cur, 0, 1, xp, st);
+            side_of<A, 2>(cur, 0, 0, xm, nullptr);
+            const double lx = xfaces_o2<A>(xp, xm, Fxlo, Fxhi);
+            if (STAGE <= STAGE_1 && xface_valid) lmax = max_nonneg(lmax, lx);
+        }
         accumulate_pair<A, true>(acc, Fxlo, Fxhi, gp.area, perx && x == nx - 1);
-        load_sides<A, 2>(gp, state, S, x, y + 1, 0, abv, (y + 1 < y1) ? st : nullptr);
-        if (out_col) {   // the halo lanes only provide x-face states
-            const double ly = side_face<A>(cur.r[1][1], abv.r[1][0], Fyhi);
-            if (STAGE <= STAGE_1) lmax = max_nonneg(lmax, ly);
+        {
+            CellRecV<1, NV> yp, ym;
+            side_of<A, 2>(cur, 1, 1, yp, st);
+            load_src<A, 2>(gp, state, S, x, y + 1, 0, cur);
+            if (out_col) {   // the halo lanes only provide x-face states
+                side_of<A, 2>(cur, 1, 0, ym, nullptr);
+                const double ly = side_face<A>(yp, ym, Fyhi);
+                if (STAGE <= STAGE_1) lmax = max_nonneg(lmax, ly);
+            }
+        }
+        if (out_col) {
             accumulate_pair<A, false>(acc, Fylo, Fyhi, gp.area, pery && y == ny - 1);
             store_output_o2<A, STAGE>(sa, gp, sc, state, (long long)x + (long long)nx * y, acc);
         }
-        cur = abv;
 #pragma unroll
         for (int k = 0; k < NV; ++k) Fylo[k] = Fyhi[k];
     }
