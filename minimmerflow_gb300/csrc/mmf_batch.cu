@@ -81,6 +81,7 @@ struct mmf_batch {
     int chunk = 32;
     int blocks_per_sm = 0;     // 0 = occupancy maximum
     int blocks = 0;
+    int slope_blocks = 0;      // the slope kernel's own grid (its occupancy maximum)
     int sms = 0;
     double *U = nullptr, *R = nullptr, *W = nullptr, *aos = nullptr;
     Ctrl *ctrl = nullptr;
@@ -133,8 +134,10 @@ struct mmf_batch {
         ob.tick = (op == BO2_SLOPES && st == STAGE_1 && indicator && ind_period > 1) ? ind_tick : nullptr;
         ++launches;
         return arith == MMF_ARITH_FAST
-                   ? launch_batch_o2_fast(op, st, cases, item_case, nitems, ctrl, base, state, ob, W, blocks, stream, w_zero)
-                   : launch_batch_o2_exact(op, st, cases, item_case, nitems, ctrl, base, state, ob, W, blocks, stream);
+                   ? launch_batch_o2_fast(op, st, cases, item_case, nitems, ctrl, base, state, ob, W,
+                                          op == BO2_SLOPES ? slope_blocks : blocks, stream, w_zero)
+                   : launch_batch_o2_exact(op, st, cases, item_case, nitems, ctrl, base, state, ob, W,
+                                           op == BO2_SLOPES ? slope_blocks : blocks, stream);
     }
     cudaError_t rk_step()
     {
@@ -202,6 +205,7 @@ static int batch_plan(mmf_batch *b, int chunk, int blocks_per_sm)
     const int maxb = batch_max_blocks_per_sm(b->arith, b->w_zero, b->order);
     b->blocks_per_sm = (blocks_per_sm > 0) ? std::min(blocks_per_sm, maxb) : maxb;
     b->blocks = b->sms * b->blocks_per_sm;
+    b->slope_blocks = b->sms * batch_slope_blocks_per_sm(b->arith, b->w_zero);
     b->drop_graphs();
     return MMF_OK;
 }

@@ -101,9 +101,16 @@ __device__ __forceinline__ void for_items(const CaseDesc *cases, const int *item
     }
 }
 
+// Minimum resident blocks per SM the batch slope kernel is compiled for; it
+// has its own grid (items are dealt to warps by for_items): five blocks of
+// four warps (at most 102 registers) for the fast arithmetic, the most
+// without spills (at six it spills 16-32 B, at eight 68-88 B).
+template <class A> struct SlopesBatchMinBlocks { static constexpr int value = 1; };
+template <int NV> struct SlopesBatchMinBlocks<FastArithT<NV>> { static constexpr int value = 5; };
+
 // slopes (computePolynomials) of the output cells of every item
 template <class A>
-__global__ void __launch_bounds__(128) slopes_batch_kernel(const CaseDesc *__restrict__ cases,
+__global__ void __launch_bounds__(128, SlopesBatchMinBlocks<A>::value) slopes_batch_kernel(const CaseDesc *__restrict__ cases,
                                                            const int *__restrict__ item_case, int nitems, Ctrl *cctrl,
                                                            const double *state, O2Batch ob, int stage)
 {
@@ -192,8 +199,8 @@ __global__ void __launch_bounds__(128, O2BatchMinBlocks<A>::value) stage2d_o2_ba
 
 enum BatchO2Op { BO2_SLOPES = 0, BO2_FORM_W1 = 1, BO2_STAGE = 2 };
 
-// Resident blocks per SM of the order-2 batch launches (the least of the
-// stage marches and the slopes, which share the persistent grid).
+// Resident blocks per SM of the order-2 batch stage marches and W1 (the
+// persistent grid they share).
 template <class A>
 inline int batch_o2_blocks_per_sm()
 {
@@ -201,8 +208,17 @@ inline int batch_o2_blocks_per_sm()
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_1>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_2>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stage2d_o2_batch_kernel<A, STAGE_3>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, slopes_batch_kernel<A>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, form_w1_batch_kernel<A>, 128, 0) == cudaSuccess) nb = v < nb ? v : nb;
     return (nb > 0 && nb < (1 << 20)) ? nb : 1;
+}
+
+// ... of the batch slope kernel (its own grid)
+template <class A>
+inline int batch_slopes_blocks_per_sm()
+{
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, slopes_batch_kernel<A>, 128, 0) != cudaSuccess || v < 1) return 1;
+    return v;
 }
 
 template <class A>
@@ -239,5 +255,6 @@ cudaError_t launch_batch_exact(int stage, const CaseDesc *cases, const int *item
 cudaError_t launch_batch_fast(int stage, const CaseDesc *cases, const int *item_case, int nitems, Ctrl *cctrl,
                               const StageArgs &base, int blocks, cudaStream_t s, bool w_zero);
 int batch_max_blocks_per_sm(int arith, bool w_zero, int order);
+int batch_slope_blocks_per_sm(int arith, bool w_zero);
 
 } // namespace mmf

@@ -31,6 +31,11 @@ cudaError_t launch_batch_o2_exact(int op, int stage, const CaseDesc *cases, cons
     return launch_batch_o2<ExactArith>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
 }
 
+int batch_slope_blocks_per_sm_exact()
+{
+    return batch_slopes_blocks_per_sm<ExactArith>();
+}
+
 int batch_max_blocks_per_sm_exact(int order)
 {
     return order == 2 ? batch_o2_blocks_per_sm<ExactArith>() : batch_blocks_per_sm<ExactArith>();

@@ -2,4 +2,5 @@
 #pragma once
 namespace mmf {
 int batch_max_blocks_per_sm_exact(int order);
+int batch_slope_blocks_per_sm_exact();
 }

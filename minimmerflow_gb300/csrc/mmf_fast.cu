@@ -38,6 +38,12 @@ cudaError_t launch_batch_o2_fast(int op, int stage, const CaseDesc *cases, const
     return launch_batch_o2<FastArith>(op, stage, cases, item_case, nitems, cctrl, base, state, ob, W1, blocks, s);
 }
 
+int batch_slope_blocks_per_sm(int arith, bool w_zero)
+{
+    if (arith == 0) return batch_slope_blocks_per_sm_exact();
+    return w_zero ? batch_slopes_blocks_per_sm<FastArith2DW0>() : batch_slopes_blocks_per_sm<FastArith>();
+}
+
 int batch_max_blocks_per_sm(int arith, bool w_zero, int order)
 {
     if (arith == 0) return batch_max_blocks_per_sm_exact(order);

@@ -134,23 +134,28 @@ __device__ __forceinline__ void load_plain(const double *planes, long long plane
     for (int k = 0; k < A::NVAR; ++k) c[k] = __ldg(planes + (long long)A::field(k) * plane + g);
 }
 
-// Positivity of the face states U -+ sigma_d / 2 of a cell, in FP64 (the
-// arithmetic's own operations).
+// Positivity of the face states U -+ sigma / 2 of one direction of a cell,
+// in FP64 (the arithmetic's own operations).
+template <class A>
+__device__ __forceinline__ bool dir_admissible(const double *uc, const double *sig)
+{
+    constexpr int NV = A::NVAR;
+    double fm[NV], fp[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        fm[k] = IsExact<A>::value ? uc[k] - 0.5 * sig[k] : fma(-0.5, sig[k], uc[k]);
+        fp[k] = face_value<A>(uc[k], 0.5, sig[k]);
+    }
+    return admissible<A>(fm) && admissible<A>(fp);
+}
+
+// ... of every direction
 template <class A, int DIM>
 __device__ __forceinline__ bool faces_admissible(const double *uc, const double (*sig)[A::NVAR])
 {
-    constexpr int NV = A::NVAR;
     bool ok = true;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        double fm[NV], fp[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            fm[k] = IsExact<A>::value ? uc[k] - 0.5 * sig[d][k] : fma(-0.5, sig[d][k], uc[k]);
-            fp[k] = face_value<A>(uc[k], 0.5, sig[d][k]);
-        }
-        ok = ok && admissible<A>(fm) && admissible<A>(fp);
-    }
+    for (int d = 0; d < DIM; ++d) ok = ok && dir_admissible<A>(uc, sig[d]);
     return ok;
 }
 
@@ -164,64 +169,74 @@ __device__ __forceinline__ float scaled_f32(double x, int emax)
     return e > 0 ? __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3)) : 0.0f;
 }
 
-// The positivity test of faces_admissible decided in FP32 where the margins
+// The positivity test of dir_admissible decided in FP32 where the margins
 // allow it: 1 = every face state has rho > 0 and 2 rho E > |m|^2, 0 = some
 // face state has not, -1 = undecided.  FP64 instructions cost about as much
 // as 30 FP32 ones on this GPU, so the FP32 screen with an FP64 fallback for
 // the undecided cells is the cheaper route to the same answer.
 //
-// The cell's values are scaled by a common power of two and truncated
-// (scaled_f32).  Each FP32 face value carries a bound e_k at least 3.7 times
-// its distance to the FP64 face value (truncation 2^-20, FP32 rounding 2^-24,
-// FP64 rounding 2^-53, relative to |u| + |sigma|/2; flushing, absolute), and
-// the bound of Q = 2 rho E - |m|^2 doubles the propagated error and adds 2^-20
-// of the magnitudes for the roundings of Q itself (FP32, and FP64 in the
-// test it replaces) and 2^-100 for underflowed terms.  A sign decided
-// outside these bounds is the sign of the FP64 evaluation.
-template <class A, int DIM>
-__device__ __forceinline__ int screen_faces(const double *uc, const double (*sig)[A::NVAR])
+// The cell's values and the direction's slopes are scaled by a common power
+// of two and truncated (scaled_f32).  Each FP32 face value carries a bound
+// e_k at least 3.7 times its distance to the FP64 face value (truncation
+// 2^-20, FP32 rounding 2^-24, FP64 rounding 2^-53, relative to |u| +
+// |sigma|/2; flushing, absolute), and the bound of Q = 2 rho E - |m|^2
+// doubles the propagated error and adds 2^-20 of the magnitudes for the
+// roundings of Q itself (FP32, and FP64 in the test it replaces) and 2^-100
+// for underflowed terms.  A sign decided outside these bounds is the sign of
+// the FP64 evaluation.
+template <class A>
+__device__ __forceinline__ int screen_dir(const double *uc, const double *sig)
 {
     constexpr int NV = A::NVAR;
     constexpr int IE = NV - 1;
     int emax = 0;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) emax = max(emax, (int)((dbits(uc[k]) >> 52) & 0x7ff));
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) emax = max(emax, (int)((dbits(sig[d][k]) >> 52) & 0x7ff));
+    for (int k = 0; k < NV; ++k) {
+        emax = max(emax, (int)((dbits(uc[k]) >> 52) & 0x7ff));
+        emax = max(emax, (int)((dbits(sig[k]) >> 52) & 0x7ff));
+    }
     if (emax >= 0x7ff) return -1;   // an infinity or a NaN
-    float u[NV], au[NV];
+    float u[NV], au[NV], sg[NV], e[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) { u[k] = scaled_f32(uc[k], emax); au[k] = fabsf(u[k]); }
+    for (int k = 0; k < NV; ++k) {
+        u[k] = scaled_f32(uc[k], emax);
+        au[k] = fabsf(u[k]);
+        sg[k] = scaled_f32(sig[k], emax);
+        e[k] = fmaf(0x1p-18f, fmaf(0.5f, fabsf(sg[k]), au[k]), 0x1p-120f);
+    }
     bool sure_ok = true, sure_bad = false;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        float sg[NV], e[NV];
+    for (int side = 0; side < 2; ++side) {
+        float f[NV], af[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            sg[k] = scaled_f32(sig[d][k], emax);
-            e[k] = fmaf(0x1p-18f, fmaf(0.5f, fabsf(sg[k]), au[k]), 0x1p-120f);
+        for (int k = 0; k < NV; ++k) { f[k] = fmaf(side ? 0.5f : -0.5f, sg[k], u[k]); af[k] = fabsf(f[k]); }
+        float m2 = 0.0f, em = 0.0f;
+#pragma unroll
+        for (int k = 1; k < IE; ++k) {
+            m2 = fmaf(f[k], f[k], m2);
+            em = fmaf(e[k], fmaf(2.0f, af[k], e[k]), em);
         }
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            float f[NV], af[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) { f[k] = fmaf(side ? 0.5f : -0.5f, sg[k], u[k]); af[k] = fabsf(f[k]); }
-            float m2 = 0.0f, em = 0.0f;
-#pragma unroll
-            for (int k = 1; k < IE; ++k) {
-                m2 = fmaf(f[k], f[k], m2);
-                em = fmaf(e[k], fmaf(2.0f, af[k], e[k]), em);
-            }
-            const float Q = fmaf(2.0f * f[0], f[IE], -m2);
-            const float eQ = fmaf(2.0f, fmaf(2.0f, fmaf(e[0], af[IE], fmaf(e[IE], af[0], e[0] * e[IE])), em),
-                                  fmaf(0x1p-20f, fmaf(2.0f * af[0], af[IE], m2), 0x1p-100f));
-            sure_ok = sure_ok && (f[0] > e[0]) && (Q > eQ);
-            sure_bad = sure_bad || (f[0] < -e[0]) || (Q < -eQ);
-        }
+        const float Q = fmaf(2.0f * f[0], f[IE], -m2);
+        const float eQ = fmaf(2.0f, fmaf(2.0f, fmaf(e[0], af[IE], fmaf(e[IE], af[0], e[0] * e[IE])), em),
+                              fmaf(0x1p-20f, fmaf(2.0f * af[0], af[IE], m2), 0x1p-100f));
+        sure_ok = sure_ok && (f[0] > e[0]) && (Q > eQ);
+        sure_bad = sure_bad || (f[0] < -e[0]) || (Q < -eQ);
     }
     return sure_bad ? 0 : (sure_ok ? 1 : -1);
+}
+
+// ... of every direction: 0 if a direction's is 0, 1 if every one's is 1
+template <class A, int DIM>
+__device__ __forceinline__ int screen_faces(const double *uc, const double (*sig)[A::NVAR])
+{
+    int dec = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const int r = screen_dir<A>(uc, sig[d]);
+        if (r == 0) return 0;
+        if (r < 0) dec = -1;
+    }
+    return dec;
 }
 
 // Self-test of screen_faces: for each sample, the FP32 decision and the FP64
@@ -256,7 +271,10 @@ inline cudaError_t launch_screen_selftest(int dim, long long n, const double *uc
 }
 
 // computePolynomials of grid cell g (index inside the grid; field planes of
-// the grid are gp.plane apart).
+// the grid are gp.plane apart).  One direction at a time: its neighbours,
+// its slopes, their positivity test (the face states of a direction depend
+// on its slopes only) and their store; a failed test in any direction sets
+// every slope of the cell to zero (order 1), the rest are not evaluated.
 template <class A, int DIM>
 __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &oa, long long g)
 {
@@ -268,28 +286,36 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
     double uc[NV];
     load_plain<A>(oa.state, n, g, uc);
     const bool limit = (oa.limit_mode == LIMIT_ALL) || (oa.limit_mode == LIMIT_FLAGGED && oa.flag[g]);
-    bool act = false;
+    // positivity fallback, also for the cells a flag leaves on central
+    // slopes; decided in FP32 where the margins allow, else in FP64
+    const bool screen = limit || oa.limit_mode == LIMIT_FLAGGED;
+    bool act = false, ok = true;
     const bool track = oa.active != nullptr;
     // fast arithmetic: the activity threshold as the bit pattern of a non-negative double
     const long long act_thr = (IsExact<A>::value || !track) ? 0 : abs_bits(1e-6 * (fabs(uc[0]) + fabs(uc[NV - 1])));
-    double sig[DIM][NV];
-#pragma unroll
+    // one direction at a time (not unrolled: only one direction's values are live)
+#pragma unroll 1
     for (int d = 0; d < DIM; ++d) {
-        double ul[NV], ur[NV];
+        if (!ok) break;
+        double ul[NV], ur[NV], sig[NV];
+        const int id = d == 0 ? idx[0] : (d == 1 ? idx[1] : idx[2]);
+        const int nd = d == 0 ? gp.n[0] : (d == 1 ? gp.n[1] : gp.n[2]);
+        const bool per = (d == 0 ? gp.bc_lo[0] : (d == 1 ? gp.bc_lo[1] : gp.bc_lo[2])) == BC_PERIODIC;
+        const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
         for (int s = 0; s < 2; ++s) {
             double *u = s ? ur : ul;
-            const int q = idx[d] + (s ? 1 : -1);
-            const bool per = gp.bc_lo[d] == BC_PERIODIC;
-            const long long stride = (d == 0) ? 1 : (d == 1) ? nx : (long long)nx * ny;
-            if (q >= 0 && q < gp.n[d]) {
+            const int q = id + (s ? 1 : -1);
+            if (q >= 0 && q < nd) {
                 load_plain<A>(oa.state, n, g + (s ? stride : -stride), u);
             } else if (per) {
-                const long long wrap = (long long)(gp.n[d] - 1) * stride;
+                const long long wrap = (long long)(nd - 1) * stride;
                 load_plain<A>(oa.state, n, s ? g - wrap : g + wrap, u);
             } else {
 #pragma unroll
                 for (int k = 0; k < NV; ++k) u[k] = uc[k];
-                ghost_in_place<A, true>(s ? gp.bc_hi[d] : gp.bc_lo[d], d, s ? 1 : -1, u, gp.dir_cons);
+                const int bc = s ? (d == 0 ? gp.bc_hi[0] : (d == 1 ? gp.bc_hi[1] : gp.bc_hi[2]))
+                                 : (d == 0 ? gp.bc_lo[0] : (d == 1 ? gp.bc_lo[1] : gp.bc_lo[2]));
+                ghost_in_place<A, true>(bc, d, s ? 1 : -1, u, gp.dir_cons);
             }
         }
 #pragma unroll
@@ -310,27 +336,24 @@ __device__ __forceinline__ void slopes_cell(const GridParams &gp, const O2Args &
                     if (track) act |= abs_bits(sl - central) > act_thr;
                 }
             }
-            sig[d][k] = sl;
+            sig[k] = sl;
+        }
+        if (screen) {
+            const int dec = screen_dir<A>(uc, sig);
+            ok = dec > 0 || (dec < 0 && dir_admissible<A>(uc, sig));
+        }
+        if (ok) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = sig[k];
         }
     }
-    if (limit || oa.limit_mode == LIMIT_FLAGGED) {
-        // positivity fallback, also for the cells a flag leaves on central
-        // slopes; decided in FP32 where the margins allow, else in FP64
-        const int dec = screen_faces<A, DIM>(uc, sig);
-        bool ok = dec > 0;
-        if (dec < 0) ok = faces_admissible<A, DIM>(uc, sig);
-        if (!ok) {
+    if (!ok) {
 #pragma unroll
-            for (int d = 0; d < DIM; ++d)
+        for (int d = 0; d < DIM; ++d)
 #pragma unroll
-                for (int k = 0; k < NV; ++k) sig[d][k] = 0.0;
-            act = true;
-        }
+            for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = 0.0;
+        act = true;
     }
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) oa.S[(long long)(d * NV + k) * n + g] = sig[d][k];
     if (oa.active) oa.active[g] = act ? 1 : 0;
 }
 
@@ -340,9 +363,14 @@ __device__ __forceinline__ bool o2_step_active(const Ctrl *ctrl, int stage)
     return (stage == 1) ? (ctrl->t < ctrl->t_end) && (ctrl->step < ctrl->max_steps) : ctrl->active != 0;
 }
 
+// Blocks per SM the slope kernel is compiled for: four (64 registers) for
+// the fast arithmetic, whose one-direction-at-a-time evaluation fits them.
+template <class A> struct SlopesMinBlocks { static constexpr int value = 1; };
+template <int NV> struct SlopesMinBlocks<FastArithT<NV>> { static constexpr int value = 4; };
+
 // computePolynomials over a grid: one thread per cell (grid-stride).
 template <class A, int DIM>
-__global__ void __launch_bounds__(256) slopes_kernel(GridParams gp, O2Args oa)
+__global__ void __launch_bounds__(256, SlopesMinBlocks<A>::value) slopes_kernel(GridParams gp, O2Args oa)
 {
     if (!o2_step_active(oa.ctrl, oa.stage)) return;
     // no block of this launch reads the counter
