@@ -749,6 +749,10 @@ def run_learned(args, world, rank, local, dist, steps=None, warmup=None):
         stream = torch.cuda.ExternalStream(s.stream_handle, device=torch.device("cuda", local))
         s.upload(U0)
         s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
+        # the decomposition tuned per mode (trial steps on U0, state restored)
+        out.setdefault("shapes", {})[mode] = s.autotune(trial_steps=2)
+        s.upload(U0)
+        s.time_setup(case.cfl, 0.0, math.inf, 10 ** 9)
         s.advance(warmup)
         launches0 = s.launch_count
         if dist is not None:
@@ -1145,6 +1149,7 @@ def main():
                                       "ratio": r["errs"]["learned"] / r["errs"]["plain"],
                                       "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2" % args.vortex_n},
                 "indicator_trained_in_this_run": r["trained_here"],
+                "planes_per_chunk": {m: sh[0] for m, sh in o["shapes"].items()},
                 "gpu_launches": o["learned"]["launches"]}
         print(json.dumps(line))
         return
@@ -1305,6 +1310,7 @@ def main():
                                                               / rl["errs"]["plain"],
                                       "case": "3D isentropic vortex %d^3 periodic, 50 steps, order 2"
                                               % args.vortex_n},
+                "planes_per_chunk": {m: sh[0] for m, sh in o["shapes"].items()},
                 "steps": k_extra}
 
         guarded("vortex3d_256", vortex3d)
