@@ -1187,8 +1187,9 @@ def main():
     achieved = stage_bytes[dom] * ncell / r["st_mean"][dom] / 1e9
     traffic_rec = read_traffic()
     traffic = None
-    if args.order == 1 and traffic_rec and str(args.n) in traffic_rec.get("per_launch_bytes", {}):
-        traffic = traffic_rec["per_launch_bytes"][str(args.n)].get("stage%d" % dom)
+    tkey = ("3d_%d" if r["case"].dim == 3 else "%d") % args.n
+    if args.order == 1 and traffic_rec and tkey in traffic_rec.get("per_launch_bytes", {}):
+        traffic = traffic_rec["per_launch_bytes"][tkey].get("stage%d" % dom)
     fp64_ops = fp64_ops_per_cell_update_2d() if (args.workload == "sod2d" and args.order == 1) else None
     if r["tuned"][1] is not None:
         workload = dict(workload, decomposition={"rows_per_chunk" if r["case"].dim == 2 else "planes_per_chunk":
@@ -1256,11 +1257,16 @@ def main():
                               warmup=w_extra, clocks=True)
                 d3 = r3["dominant"]
                 ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
+                # ncu DRAM bytes of the captured decomposition (tile kernel, 32-plane chunks)
+                tr3 = read_traffic() or {}
+                tile32 = r3["tuned"][1] == -1 and r3["tuned"][0] == 32
+                traffic3 = tr3.get("per_launch_bytes", {}).get("3d_256", {}).get("stage%d" % d3) if tile32 else None
                 v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
                                         "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),
                                         "hbm_frac": CELL_BYTES_STEP * r3["value"] / 1e9 / hbm_peak,
                                         "dominant_stage": {"stage": d3, "achieved_gbs": ach3,
-                                                           "frac": ach3 / hbm_peak},
+                                                           "frac": ach3 / hbm_peak, "traffic": traffic3,
+                                                           "algorithmic_bytes": STAGE_BYTES[d3] * r3["ncell"]},
                                         "stage_ms": {str(k): 1e3 * v for k, v in r3["st_mean"].items()},
                                         "planes_per_chunk": r3["tuned"][0],
                                         "kernel": "tile" if r3["tuned"][1] == -1 else "row blocks",
