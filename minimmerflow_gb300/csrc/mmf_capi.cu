@@ -177,7 +177,8 @@ int mmf_create(const mmf_grid *grid, int device, mmf_ctx **out)
     gp.area = (grid->dim == 3) ? h * h : h;
     gp.vol = (grid->dim == 3) ? h * h * h : h * h;
     gp.half_area_per_vol = 0.5 * gp.area / gp.vol;
-    plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D, 0, grid->order == 1 ? TILE3D_DEFAULT : 0);
+    plan_cartesian(gp, grid->chunk, grid->order == 2 ? BY3D_O2 : BY3D, 0, grid->order == 1 ? TILE3D_DEFAULT : 0,
+                   grid->order);
     const size_t bytes = sizeof(double) * NF * (size_t)gp.plane;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->U, bytes);
@@ -1130,7 +1131,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     const bool d2 = c->gp.dim == 2;
     std::pair<int, int> best(c->gp.chunk, d2 ? c->gp.wpb : c->gp.tile3d);
     for (const auto &cd : cand) {
-        plan_cartesian(c->gp, cd.first, by, d2 ? cd.second : 0, d2 ? 0 : cd.second);
+        plan_cartesian(c->gp, cd.first, by, d2 ? cd.second : 0, d2 ? 0 : cd.second, c->grid.order);
         e = cudaMemcpyAsync(c->U, c->aos, bytes, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->ctrl, &trial, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = c->rk_step();
@@ -1145,7 +1146,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    plan_cartesian(c->gp, best.first, by, d2 ? best.second : 0, d2 ? 0 : best.second);
+    plan_cartesian(c->gp, best.first, by, d2 ? best.second : 0, d2 ? 0 : best.second, c->grid.order);
     if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
     if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
     MMF_CUDA(e);
@@ -1168,7 +1169,8 @@ int mmf_set_shape(mmf_ctx *c, int chunk, int variant)
     if (!d2 && variant != 0 && variant != 1) return fail(MMF_ERR_ARG, "3D: variant must be 0 (row blocks) or 1 (tiles)");
     if (!d2 && variant == 1 && c->grid.order != 1) return fail(MMF_ERR_UNSUPPORTED, "the 3D tile kernel is order 1");
     MMF_CUDA(cudaStreamSynchronize(c->stream));
-    plan_cartesian(c->gp, chunk, c->grid.order == 2 ? BY3D_O2 : BY3D, d2 ? variant : 0, d2 ? 0 : variant);
+    plan_cartesian(c->gp, chunk, c->grid.order == 2 ? BY3D_O2 : BY3D, d2 ? variant : 0, d2 ? 0 : variant,
+                   c->grid.order);
     if (c->graph_many) { cudaGraphExecDestroy(c->graph_many); c->graph_many = nullptr; }
     if (c->graph_one) { cudaGraphExecDestroy(c->graph_one); c->graph_one = nullptr; }
     return MMF_OK;

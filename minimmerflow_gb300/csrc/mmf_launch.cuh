@@ -19,10 +19,12 @@ constexpr int TILE3D_DEFAULT = 1;   // order-1 3D kernel when nothing else is ch
 
 // Fills the decomposition fields of gp for the given marching chunk; 'by' is
 // the number of warps a 3D block stacks in y (two of them halo rows) in the
-// row-block kernel; tile3d selects the 3D tile kernel (order 1 only).
-inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0, int tile3d = 0)
+// row-block kernel; tile3d selects the 3D tile kernel (order 1 only); order 2
+// in 3D has rows of SEG3D_O2 output columns.
+inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0, int tile3d = 0, int order = 1)
 {
-    gp.nseg = (gp.n[0] + SEG - 1) / SEG;
+    const int seg = (gp.dim == 3 && order == 2) ? SEG3D_O2 : SEG;
+    gp.nseg = (gp.n[0] + seg - 1) / seg;
     gp.wpb = (wpb >= 1 && wpb <= WARPS_2D) ? wpb : WARPS_2D;
     gp.tile3d = (gp.dim == 3 && tile3d) ? 1 : 0;
     gp.chunk0 = 0;

@@ -614,12 +614,20 @@ __global__ void __launch_bounds__(128) stage2d_o2_kernel(GridParams gp, StageArg
 }
 
 // ---------------------------------------------------------------- 3D, order 2
+// The 3D kernel's rows are 32 output columns wide (every lane an output
+// cell, so 256 columns take 8 rows exactly); the face sides of the columns
+// left and right of a row come from the block's two halo warps.
+constexpr int SEG3D_O2 = 32;
+
 template <int BY, int NV>
 struct Smem3DO2 {
     double c[BY][NV][32];
     double f[BY][NV][32];
     double lam[BY][32];
     double F[BY][NV][32];
+    // x-halo face sides per row: [0] the +x side of the column left of the
+    // block, [1] the -x side of the column right of it
+    double xc[2][NV][BY], xf[2][NV][BY], xlam[2][BY];
 };
 
 // Registers: the next plane is kept as its state and slopes (SideSrc), and
@@ -645,13 +653,14 @@ __global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A, BY>::value)
     const int seg = b % gp.nseg; b /= gp.nseg;
     const int rb = b % gp.nrowblk; b /= gp.nrowblk;
     const int chunk = gp.chunk0 + b;
-    const int x = seg * SEG - 1 + lane;
+    const int x0 = seg * SEG3D_O2;
+    const int x = x0 + lane;
     const int y = rb * (BY - 2) - 1 + w;
     const int z0 = chunk * gp.chunk;
     const int z1 = min(z0 + gp.chunk, nz);
     const bool halo_lo = (w == 0), halo_hi = (w == BY - 1);
     const bool out_row = !halo_lo && !halo_hi && (y < ny);
-    const bool out_col = (lane >= 1) && (lane <= SEG) && (x < nx);
+    const bool out_col = x < nx;
     const bool out = out_row && out_col;
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
                perz = gp.bc_lo[2] == BC_PERIODIC;
@@ -662,8 +671,31 @@ __global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A, BY>::value)
     unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
     double lmax = 0.0;
 
+    // The x-halo face sides of the output rows of plane zz, by the halo
+    // warps: lane r of the low one the +x side of the cell left of row r, of
+    // the high one the -x side of the cell right of it.  Written for plane
+    // z + 1 between the second and third barriers of plane z, read before the
+    // first barrier of plane z + 1.
+    auto x_halo = [&](int zz) {
+        const int yr = rb * (BY - 2) - 1 + lane;
+        if (lane >= 1 && lane <= BY - 2 && yr < ny) {
+            const int side = halo_lo ? 0 : 1;
+            CellRecV<1, NV> xr;
+            {
+                SideSrc<A, 3> h;
+                load_src<A, 3>(gp, state, S, halo_lo ? x0 - 1 : x0 + SEG3D_O2, yr, zz, h);
+                side_of<A, 3>(h, 0, halo_lo ? 1 : 0, xr, nullptr);
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) { sm.xc[side][k][lane] = xr.c[k]; sm.xf[side][k][lane] = xr.f[0][k]; }
+            sm.xlam[side][lane] = xr.lam[0];
+        }
+    };
+
     SideSrc<A, 3> cur;
     double Fzlo[NV], Fzhi[NV], Fa[NV], Fb[NV], acc[NV];
+    if (halo_lo || halo_hi) x_halo(z0);
+    __syncthreads();
     if (!halo_lo && !halo_hi && !idle) {
         CellRecV<1, NV> below, zm;
         {
@@ -677,9 +709,10 @@ __global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A, BY>::value)
         if (out) lmax = max_nonneg(lmax, l);
     }
     for (int z = z0; z < z1; ++z) {
-        if (idle) {   // the three barriers of a plane
+        if (idle) {   // the three barriers of a plane (an idle high halo warp still makes the x halo)
             __syncthreads();
             __syncthreads();
+            if (halo_hi && z + 1 < z1) x_halo(z + 1);
             __syncthreads();
             continue;
         }
@@ -706,15 +739,37 @@ __global__ void __launch_bounds__(BY * 32, O2Stage3DMinBlocks<A, BY>::value)
                 if (STAGE <= STAGE_1 && out_col && y - 1 < ny) lmax = max_nonneg(lmax, ly);
             }
             __syncthreads();
+            if (z + 1 < z1) x_halo(z + 1);   // read after the next plane's start
             __syncthreads();
             continue;
         }
+        // x faces: the right one with the next lane's -x side (lane 31: the
+        // right halo column's), the left one the previous lane's right face
+        // (lane 0: evaluated with the left halo column's +x side)
         {
-            CellRecV<1, NV> xp, xm;
+            CellRecV<1, NV> xp, xm, R;
             side_of<A, 3>(cur, 0, 1, xp, st);
             side_of<A, 3>(cur, 0, 0, xm, nullptr);
-            const double lx = xfaces_o2<A>(xp, xm, Fa, Fb);
-            if (STAGE <= STAGE_1 && out_row && lane <= SEG && x < nx) lmax = max_nonneg(lmax, lx);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double c = shfl_down(xm.c[k], 1), f = shfl_down(xm.f[0][k], 1);
+                R.c[k] = lane == 31 ? sm.xc[1][k][w] : c;
+                R.f[0][k] = lane == 31 ? sm.xf[1][k][w] : f;
+            }
+            const double lr = shfl_down(xm.lam[0], 1);
+            R.lam[0] = lane == 31 ? sm.xlam[1][w] : lr;
+            const double lx = side_face<A>(xp, R, Fb);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lx);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) Fa[k] = shfl_up(Fb[k], 1);
+            if (lane == 0) {
+                CellRecV<1, NV> L;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) { L.c[k] = sm.xc[0][k][w]; L.f[0][k] = sm.xf[0][k][w]; }
+                L.lam[0] = sm.xlam[0][w];
+                const double ll = side_face<A>(L, xm, Fa);
+                if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ll);
+            }
         }
         accumulate_pair<A, true>(acc, Fa, Fb, gp.area, perx && x == nx - 1);
         // y faces: rows publish their +y side, each row evaluates the face below it
