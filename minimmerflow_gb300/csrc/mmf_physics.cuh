@@ -246,15 +246,18 @@ struct FastArithT {
         if (status) *status |= state_flags(rho, p);
         const double a = sqrt_newton(GAMMA * p * rinv);
         const double H = E + p;                             // rho * total enthalpy
+        // the momentum fluxes rho u_i u_j (i != j) once each
         const double muv = r.c[1] * v;                      // rho u v
+        const double muw = (NV == 5) ? r.c[1] * w : 0.0;    // rho u w
+        const double mvw = (NV == 5) ? r.c[2] * w : 0.0;    // rho v w
         const double vel[3] = {u, v, w};
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
             const double m = r.c[1 + d];
             r.f[d][0] = m;
-            r.f[d][1] = (d == 0) ? fma(m, u, p) : (d == 1 ? muv : m * u);
-            r.f[d][2] = (d == 1) ? fma(m, v, p) : (d == 0 ? muv : m * v);
-            if (NV == 5) r.f[d][3] = (d == 2) ? fma(m, w, p) : m * w;
+            r.f[d][1] = (d == 0) ? fma(m, u, p) : (d == 1 ? muv : muw);
+            r.f[d][2] = (d == 1) ? fma(m, v, p) : (d == 0 ? muv : mvw);
+            if (NV == 5) r.f[d][3] = (d == 2) ? fma(m, w, p) : (d == 0 ? muw : mvw);
             r.f[d][IE] = vel[d] * H;
             r.lam[d] = fabs(vel[d]) + a;
         }
