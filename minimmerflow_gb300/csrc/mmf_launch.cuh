@@ -14,7 +14,7 @@ namespace mmf {
 
 constexpr int BY3D = 16;        // warps per 3D block (14 output rows + 2 halo rows)
 constexpr int WARPS_2D = 4;     // warps per 2D block
-constexpr int BY3D_O2 = 8;      // warps per 3D order-2 block (face-side records need twice the registers)
+constexpr int BY3D_O2 = 16;     // warps per 3D order-2 block (14 output rows + 2 halo rows)
 constexpr int TILE3D_DEFAULT = 1;   // order-1 3D kernel when nothing else is chosen: the tile kernel
 
 // Fills the decomposition fields of gp for the given marching chunk; 'by' is
