@@ -632,7 +632,7 @@ struct Smem3DO2 {
 
 // Registers: the next plane is kept as its state and slopes (SideSrc), and
 // each face-side record is evaluated where its face is, so that the kernel
-// fits 128 registers: two blocks of 8 warps (one of 16) per SM.
+// fits 128 registers: one block of 16 warps (or two of 8) per SM.
 template <class A, int BY> struct O2Stage3DMinBlocks { static constexpr int value = 1; };
 template <int BY> struct O2Stage3DMinBlocks<FastArithT<5>, BY> { static constexpr int value = BY <= 8 ? 2 : 1; };
 
