@@ -60,7 +60,8 @@ static cudaError_t launch_infer(mmf_mlp *p, const GridParams &gp, const float *Q
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long ntiles = (gp.plane + MLP_TILE - 1) / MLP_TILE;
-    const int blocks = (int)(ntiles < (long long)MLP_CTAS_PER_SM * sms ? ntiles : (long long)MLP_CTAS_PER_SM * sms);
+    const long long slots = (long long)mlp_ctas_per_sm(DIM) * sms;
+    const int blocks = (int)(ntiles < slots ? ntiles : slots);
     MlpDev w;
     w.w1c = p->w1c;
     w.w2c = p->w2c;

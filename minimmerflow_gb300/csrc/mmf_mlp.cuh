@@ -43,7 +43,9 @@ namespace mmf {
 
 constexpr int MLP_H = 64;            // hidden width
 constexpr int MLP_TILE = 128;        // cells per tcgen05 tile (M)
-constexpr int MLP_CTAS_PER_SM = 3;   // inference CTAs per SM (shared memory, registers, 3 x 128 TMEM columns)
+// inference CTAs per SM (shared memory, registers, 128 of the 512 TMEM
+// columns each): four in 2D (48 features), three in 3D (144)
+__host__ __device__ constexpr int mlp_ctas_per_sm(int dim) { return dim == 2 ? 4 : 3; }
 
 __host__ __device__ constexpr int mlp_kin(int dim) { return dim == 3 ? 135 : 45; }
 __host__ __device__ constexpr int mlp_kpad(int dim) { return dim == 3 ? 144 : 48; }
@@ -365,7 +367,7 @@ struct WaitLimits {
 // Sets *err when a wait gave up: 1 an MMA completion, 2 the weights' copies,
 // 3 the probe barrier (WaitLimits).
 template <int DIM, int SRC>
-__global__ void __launch_bounds__(128, MLP_CTAS_PER_SM) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
+__global__ void __launch_bounds__(128, mlp_ctas_per_sm(DIM)) mlp_infer_kernel(GridParams gp, const float *Q, const __nv_bfloat16 *X,
                                                            MlpDev w, float threshold, float *prob,
                                                            unsigned char *flags, int *err, BatchGeom bg,
                                                            WaitLimits lim, IndicatorStep is)
