@@ -1074,7 +1074,8 @@ def main():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--variant", type=int, default=-1,
-                    help="with --chunk: 2D warps per block, 3D kernel (0 row blocks, 1 tiles)")
+                    help="with --chunk: 2D warps per block, 3D kernel (0 row blocks, 1 tiles one block per "
+                         "tile and chunk, 2 tiles one block per resident slot)")
     ap.add_argument("--order", type=int, default=1, choices=[1, 2])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--cpu-procs", type=int, default=0)
@@ -1188,6 +1189,10 @@ def main():
     traffic_rec = read_traffic()
     traffic = None
     tkey = ("3d_%d" if r["case"].dim == 3 else "%d") % args.n
+    if r["case"].dim == 3:
+        # the captured 3D decompositions: tiles with one block per tile and
+        # 32-plane chunk, and on one block per resident slot with 128-plane units
+        tkey = {(-1, 32): tkey, (-2, 128): tkey + "_slots"}.get((r["tuned"][1], r["tuned"][0]))
     if args.order == 1 and traffic_rec and tkey in traffic_rec.get("per_launch_bytes", {}):
         traffic = traffic_rec["per_launch_bytes"][tkey].get("stage%d" % dom)
     fp64_ops = fp64_ops_per_cell_update_2d() if (args.workload == "sod2d" and args.order == 1) else None
@@ -1257,10 +1262,12 @@ def main():
                               warmup=w_extra, clocks=True)
                 d3 = r3["dominant"]
                 ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
-                # ncu DRAM bytes of the captured decomposition (tile kernel, 32-plane chunks)
+                # ncu DRAM bytes of the captured decompositions: the tile kernel
+                # with one block per tile and 32-plane chunk, or on one block per
+                # resident slot with 128-plane units
                 tr3 = read_traffic() or {}
-                tile32 = r3["tuned"][1] == -1 and r3["tuned"][0] == 32
-                traffic3 = tr3.get("per_launch_bytes", {}).get("3d_256", {}).get("stage%d" % d3) if tile32 else None
+                tkey3 = {(-1, 32): "3d_256", (-2, 128): "3d_256_slots"}.get((r3["tuned"][1], r3["tuned"][0]))
+                traffic3 = tr3.get("per_launch_bytes", {}).get(tkey3, {}).get("stage%d" % d3) if tkey3 else None
                 v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
                                         "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),
                                         "hbm_frac": CELL_BYTES_STEP * r3["value"] / 1e9 / hbm_peak,
@@ -1269,7 +1276,9 @@ def main():
                                                            "algorithmic_bytes": STAGE_BYTES[d3] * r3["ncell"]},
                                         "stage_ms": {str(k): 1e3 * v for k, v in r3["st_mean"].items()},
                                         "planes_per_chunk": r3["tuned"][0],
-                                        "kernel": "tile" if r3["tuned"][1] == -1 else "row blocks",
+                                        "kernel": {-2: "tiles, one block per resident slot",
+                                                   -1: "tiles, one block per tile and chunk"}.get(
+                                                       r3["tuned"][1], "row blocks"),
                                         "gpu_launches": r3["launches"],
                                         "e2e": {"value": r3["e2e"], "unit": metric,
                                                 "h2d_bytes_per_step": 40 * r3["ncell"],

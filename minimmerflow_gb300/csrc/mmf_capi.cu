@@ -1116,11 +1116,15 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
         for (int ch : {8, 12, 16, 20, 24, 28, 30, 32, 40, 48, 64})
             for (int w : {1, 2, 4}) cand.emplace_back(ch, w);
     } else {
-        // order 1: both 3D kernels (second = 1: tile kernel); order 2: row blocks
+        // order 1: both 3D kernels (second = 1: tile kernel, one block per
+        // tile and chunk; 2: tile kernel, at most one block per resident
+        // slot); order 2: row blocks
         for (int ch : {4, 6, 8, 12, 14, 16, 24, 32, 64}) {
             cand.emplace_back(ch, 0);
             if (c->grid.order == 1) cand.emplace_back(ch, 1);
         }
+        if (c->grid.order == 1)
+            for (int ch : {8, 16, 32, 64, 128}) cand.emplace_back(ch, 2);
     }
     const int by = c->grid.order == 2 ? BY3D_O2 : BY3D;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1155,7 +1159,7 @@ int mmf_autotune(mmf_ctx *c, int trial_steps, int *chunk_out, int *warps_out)
     c->indicator_restart();
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     if (chunk_out) *chunk_out = c->gp.chunk;
-    if (warps_out) *warps_out = d2 ? c->gp.wpb : (c->gp.tile3d ? -1 : 0);
+    if (warps_out) *warps_out = d2 ? c->gp.wpb : -c->gp.tile3d;
     return MMF_OK;
 }
 
@@ -1166,8 +1170,10 @@ int mmf_set_shape(mmf_ctx *c, int chunk, int variant)
     if (chunk < 1) return fail(MMF_ERR_ARG, "chunk must be >= 1");
     const bool d2 = c->gp.dim == 2;
     if (d2 && (variant < 1 || variant > WARPS_2D)) return fail(MMF_ERR_ARG, "2D: warps per block must be 1..4");
-    if (!d2 && variant != 0 && variant != 1) return fail(MMF_ERR_ARG, "3D: variant must be 0 (row blocks) or 1 (tiles)");
-    if (!d2 && variant == 1 && c->grid.order != 1) return fail(MMF_ERR_UNSUPPORTED, "the 3D tile kernel is order 1");
+    if (!d2 && (variant < 0 || variant > 2))
+        return fail(MMF_ERR_ARG, "3D: variant must be 0 (row blocks), 1 (tiles, one block per tile and chunk) or "
+                                 "2 (tiles, one block per resident slot)");
+    if (!d2 && variant >= 1 && c->grid.order != 1) return fail(MMF_ERR_UNSUPPORTED, "the 3D tile kernel is order 1");
     MMF_CUDA(cudaStreamSynchronize(c->stream));
     plan_cartesian(c->gp, chunk, c->grid.order == 2 ? BY3D_O2 : BY3D, d2 ? variant : 0, d2 ? 0 : variant,
                    c->grid.order);

@@ -59,7 +59,9 @@ struct GridParams {
     int chunk0;     // first chunk of the launch (a launch may cover a band of the grid)
     int bookkeep;   // this launch updates the control block (exactly one launch per stage)
     int wpb;        // 2D: warps per block
-    int tile3d;     // 3D order 1: 1 = 32 x 16 tile kernel, 0 = row-block kernel
+    int tile3d;     // 3D order 1: 0 = row-block kernel, 1 = 32 x 16 tile kernel with one block per tile and
+                    // chunk, 2 = the tile kernel on at most one block per resident slot
+    int unit;       // tile3d 2: planes per (column, unit) work unit (a band launch keeps the whole grid's)
     long long plane;  // cells per field plane
 };
 
@@ -611,117 +613,155 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
 
     const int nx = gp.n[0], ny = gp.n[1], nz = gp.n[2];
     const int ntx = (nx + TILE_X - 1) / TILE_X, nty = (ny + TILE_Y - 1) / TILE_Y;
-    int b = blockIdx.x;
-    const int tx = b % ntx; b /= ntx;
-    const int ty = b % nty; b /= nty;
-    const int chunk = gp.chunk0 + b;
-    const int x0 = tx * TILE_X, y0 = ty * TILE_Y;
-    const int x = x0 + l, y = y0 + w;
-    const int z0 = chunk * gp.chunk;
-    const int z1 = min(z0 + gp.chunk, nz);
-    const bool out = (x < nx) && (y < ny);
     const bool perx = gp.bc_lo[0] == BC_PERIODIC, pery = gp.bc_lo[1] == BC_PERIODIC,
                perz = gp.bc_lo[2] == BC_PERIODIC;
+    // The launch covers planes [zlo, zlo + nzr) of every tile column, as
+    // units of one column and L planes, columns fastest.  With G blocks, the
+    // whole rounds of G units go one unit per block (block b: units b, b + G,
+    // ...), so the blocks running together march neighbouring columns over
+    // the same planes and their halo rows and columns are read from L2; the
+    // units of the last, partial round are split evenly over all G blocks as
+    // (column, plane) pairs, unit after unit.  One block per chunk-long unit
+    // (G = units) is the plain one-chunk-per-block decomposition.
+    const int ntiles = ntx * nty, G = gridDim.x;
+    const int zlo = gp.chunk0 * gp.chunk;
+    const int nzr = min(nz, zlo + gp.nchunk * gp.chunk) - zlo;
+    const int L = (gp.tile3d == 2 && gp.unit > 0) ? gp.unit : gp.chunk;
+    const int nunit = (nzr + L - 1) / L;                     // units per column
+    const int units = ntiles * nunit;
+    const int full = units / G * G;
+    const int last_len = nzr - (nunit - 1) * L;              // planes of a column's last unit
+    const int ub = (nunit - 1) * ntiles;                     // first unit of the columns' last units
+    const int na = max(0, ub - full);                        // tail units of L planes
+    const int nb = units - max(full, ub);                    // tail units of last_len planes
+    const long long npair = (long long)na * L + (long long)nb * last_len;
+    int q = (int)(npair * blockIdx.x / G);
+    const int q1 = (int)(npair * (blockIdx.x + 1) / G);
+    int u = blockIdx.x;
     unsigned status = 0;
-    unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
     double lmax = 0.0;
+    for (;;) {
+        int col, z0, z1;
+        if (u < full) {
+            col = u % ntiles;
+            z0 = zlo + (u / ntiles) * L;
+            z1 = min(z0 + L, zlo + nzr);
+            u += G;
+        } else if (q < q1) {
+            const bool a = q < na * L;
+            const int len = a ? L : last_len;
+            const int qq = a ? q : q - na * L;
+            const int uu = (a ? full : max(full, ub)) + qq / len;
+            const int off = qq - (qq / len) * len;
+            col = uu % ntiles;
+            z0 = zlo + (uu / ntiles) * L + off;
+            z1 = z0 + min(len - off, q1 - q);
+            q += z1 - z0;
+        } else {
+            break;
+        }
+        const int x0 = (col % ntx) * TILE_X, y0 = (col / ntx) * TILE_Y;
+        const int x = x0 + l, y = y0 + w;
+        const bool out = (x < nx) && (y < ny);
+        unsigned *st = (STAGE == STAGE_1 && out) ? &status : nullptr;
 
-    RecOf<A, 3> cur, nxt;
-    double Fzlo[NV], Fzhi[NV], Fxl[NV], Fxr[NV], Fyb[NV], Fyt[NV], acc[NV];
-    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, nxt, nullptr);
-    load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
-    {
-        const double lz = face_dir<A, 3>(nxt, cur, 2, Fzlo);
-        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
-    }
-    tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z0);
-    tile_publish<NV>(sm, cur, w, l);
-    for (int z = z0; z < z1; ++z) {
-        __syncthreads();   // (A) records of plane z
-        // x face on the right: the next lane (lane 31's, on the tile's right
-        // edge, comes from the edge pass; its value here is replaced)
+        RecOf<A, 3> cur, nxt;
+        double Fzlo[NV], Fzhi[NV], Fxl[NV], Fxr[NV], Fyb[NV], Fyt[NV], acc[NV];
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0 - 1, nxt, nullptr);
+        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z0, cur, st);
         {
-            double cR[NV], fR[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) { cR[k] = shfl_down(cur.c[k], 1); fR[k] = shfl_down(cur.f[0][k], 1); }
-            const double lamR = shfl_down(cur.lam[0], 1);
-            const double lx = A::face(cur.c, cur.f[0], cur.lam[0], cR, fR, lamR, Fxr);
-            if (STAGE <= STAGE_1 && out && l < 31) lmax = max_nonneg(lmax, lx);
+            const double lz = face_dir<A, 3>(nxt, cur, 2, Fzlo);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
         }
-        // y face above: the next row, or the top halo row
-        {
-            double cU[NV], fU[NV];
+        tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z0);
+        tile_publish<NV>(sm, cur, w, l);
+        for (int z = z0; z < z1; ++z) {
+            __syncthreads();   // (A) records of plane z
+            // x face on the right: the next lane (lane 31's, on the tile's right
+            // edge, comes from the edge pass; its value here is replaced)
+            {
+                double cR[NV], fR[NV];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) { cU[k] = sm.yc[w + 1][k][l]; fU[k] = sm.yf[w + 1][k][l]; }
-            const double ly = A::face(cur.c, cur.f[1], cur.lam[1], cU, fU, sm.ylam[w + 1][l], Fyt);
-            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
+                for (int k = 0; k < NV; ++k) { cR[k] = shfl_down(cur.c[k], 1); fR[k] = shfl_down(cur.f[0][k], 1); }
+                const double lamR = shfl_down(cur.lam[0], 1);
+                const double lx = A::face(cur.c, cur.f[0], cur.lam[0], cR, fR, lamR, Fxr);
+                if (STAGE <= STAGE_1 && out && l < 31) lmax = max_nonneg(lmax, lx);
+            }
+            // y face above: the next row, or the top halo row
+            {
+                double cU[NV], fU[NV];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) sm.Fy[w][k][l] = Fyt[k];
-        }
-        // faces on the tile's left edge (lanes 0..15: rows), right edge (lanes
-        // 16..31: rows) and bottom edge (lanes: columns)
-        if (w == TW_LEFTF) {
-            const int r = l & 15;
-            const bool right = l >= 16;
-            double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
+                for (int k = 0; k < NV; ++k) { cU[k] = sm.yc[w + 1][k][l]; fU[k] = sm.yf[w + 1][k][l]; }
+                const double ly = A::face(cur.c, cur.f[1], cur.lam[1], cU, fU, sm.ylam[w + 1][l], Fyt);
+                if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, ly);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.Fy[w][k][l] = Fyt[k];
+            }
+            // faces on the tile's left edge (lanes 0..15: rows), right edge (lanes
+            // 16..31: rows) and bottom edge (lanes: columns)
+            if (w == TW_LEFTF) {
+                const int r = l & 15;
+                const bool right = l >= 16;
+                double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    cL[k] = right ? sm.c31[k][r] : sm.xc[0][k][r];
+                    fL[k] = right ? sm.f31[k][r] : sm.xf[0][k][r];
+                    cR[k] = right ? sm.xc[1][k][r] : sm.c0[k][r];
+                    fR[k] = right ? sm.xf[1][k][r] : sm.f0[k][r];
+                }
+                const double le = A::face(cL, fL, right ? sm.lam31[r] : sm.xlam[0][r], cR, fR,
+                                          right ? sm.xlam[1][r] : sm.lam0[r], F);
+                if (right) {
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) sm.Fr[k][r] = F[k];
+                    if (STAGE <= STAGE_1 && x0 + TILE_X - 1 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) sm.Fl[k][r] = F[k];
+                    if (STAGE <= STAGE_1 && x0 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
+                }
+            } else if (w == TW_BOTF) {
+                double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    cL[k] = sm.bc[k][l]; fL[k] = sm.bf[k][l]; cR[k] = sm.yc[0][k][l]; fR[k] = sm.yf[0][k][l];
+                }
+                const double le = A::face(cL, fL, sm.blam[l], cR, fR, sm.ylam[0][l], F);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sm.Fb[k][l] = F[k];
+                if (STAGE <= STAGE_1 && x < nx && y0 < ny) lmax = max_nonneg(lmax, le);
+            }
+            __syncthreads();   // (B) faces of plane z
+            // the faces below and on the left: the previous lane / row, or the tile edge
+            const int wb = (w > 0) ? w - 1 : 0;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                cL[k] = right ? sm.c31[k][r] : sm.xc[0][k][r];
-                fL[k] = right ? sm.f31[k][r] : sm.xf[0][k][r];
-                cR[k] = right ? sm.xc[1][k][r] : sm.c0[k][r];
-                fR[k] = right ? sm.xf[1][k][r] : sm.f0[k][r];
+                const double fl = shfl_up(Fxr[k], 1);
+                Fxl[k] = (l == 0) ? sm.Fl[k][w] : fl;
+                Fxr[k] = (l == 31) ? sm.Fr[k][w] : Fxr[k];
+                Fyb[k] = (w == 0) ? sm.Fb[k][l] : sm.Fy[wb][k][l];
             }
-            const double le = A::face(cL, fL, right ? sm.lam31[r] : sm.xlam[0][r], cR, fR,
-                                      right ? sm.xlam[1][r] : sm.lam0[r], F);
-            if (right) {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) sm.Fr[k][r] = F[k];
-                if (STAGE <= STAGE_1 && x0 + TILE_X - 1 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
-            } else {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) sm.Fl[k][r] = F[k];
-                if (STAGE <= STAGE_1 && x0 < nx && y0 + r < ny) lmax = max_nonneg(lmax, le);
+            accumulate_pair<A, true>(acc, Fxl, Fxr, gp.area, perx && x == nx - 1);
+            accumulate_pair<A, false>(acc, Fyb, Fyt, gp.area, pery && y == ny - 1);
+            // plane z+1 and the z face
+            load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, nxt, (z + 1 < z1) ? st : nullptr);
+            const double lz = face_dir<A, 3>(cur, nxt, 2, Fzhi);
+            if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
+            if (out) {
+                accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
+                store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
+                                       acc, cur.c);
             }
-        } else if (w == TW_BOTF) {
-            double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                cL[k] = sm.bc[k][l]; fL[k] = sm.bf[k][l]; cR[k] = sm.yc[0][k][l]; fR[k] = sm.yf[0][k][l];
+            // records of plane z+1 for the next (A)
+            if (z + 1 < z1) {
+                tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z + 1);
+                tile_publish<NV>(sm, nxt, w, l);
             }
-            const double le = A::face(cL, fL, sm.blam[l], cR, fR, sm.ylam[0][l], F);
+            cur = nxt;
 #pragma unroll
-            for (int k = 0; k < NV; ++k) sm.Fb[k][l] = F[k];
-            if (STAGE <= STAGE_1 && x < nx && y0 < ny) lmax = max_nonneg(lmax, le);
+            for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
         }
-        __syncthreads();   // (B) faces of plane z
-        // the faces below and on the left: the previous lane / row, or the tile edge
-        const int wb = (w > 0) ? w - 1 : 0;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            const double fl = shfl_up(Fxr[k], 1);
-            Fxl[k] = (l == 0) ? sm.Fl[k][w] : fl;
-            Fxr[k] = (l == 31) ? sm.Fr[k][w] : Fxr[k];
-            Fyb[k] = (w == 0) ? sm.Fb[k][l] : sm.Fy[wb][k][l];
-        }
-        accumulate_pair<A, true>(acc, Fxl, Fxr, gp.area, perx && x == nx - 1);
-        accumulate_pair<A, false>(acc, Fyb, Fyt, gp.area, pery && y == ny - 1);
-        // plane z+1 and the z face
-        load_record<A, STAGE, 3>(sa, gp, sc, x, y, z + 1, nxt, (z + 1 < z1) ? st : nullptr);
-        const double lz = face_dir<A, 3>(cur, nxt, 2, Fzhi);
-        if (STAGE <= STAGE_1 && out) lmax = max_nonneg(lmax, lz);
-        if (out) {
-            accumulate_pair<A, false>(acc, Fzlo, Fzhi, gp.area, perz && z == nz - 1);
-            store_output<A, STAGE>(sa, gp, sc, (long long)x + (long long)nx * ((long long)y + (long long)ny * z),
-                                   acc, cur.c);
-        }
-        // records of plane z+1 for the next (A)
-        if (z + 1 < z1) {
-            tile_halo_records<A, STAGE>(sa, gp, sc, sm, w, l, x0, y0, z + 1);
-            tile_publish<NV>(sm, nxt, w, l);
-        }
-        cur = nxt;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) Fzlo[k] = Fzhi[k];
     }
     publish_reductions<STAGE>(lmax, status, sa.ctrl, sa.rhs_maxeig);
 }

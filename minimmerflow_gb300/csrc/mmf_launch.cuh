@@ -15,20 +15,25 @@ namespace mmf {
 constexpr int BY3D = 16;        // warps per 3D block (14 output rows + 2 halo rows)
 constexpr int WARPS_2D = 4;     // warps per 2D block
 constexpr int BY3D_O2 = 16;     // warps per 3D order-2 block (14 output rows + 2 halo rows)
-constexpr int TILE3D_DEFAULT = 1;   // order-1 3D kernel when nothing else is chosen: the tile kernel
+// order-1 3D kernel when nothing else is chosen: the tile kernel, one block
+// per resident slot
+constexpr int TILE3D_DEFAULT = 2;
 
 // Fills the decomposition fields of gp for the given marching chunk; 'by' is
 // the number of warps a 3D block stacks in y (two of them halo rows) in the
-// row-block kernel; tile3d selects the 3D tile kernel (order 1 only); order 2
-// in 3D has rows of SEG3D_O2 output columns.
+// row-block kernel; tile3d selects the 3D tile kernel (order 1 only: 1 = one
+// block per tile and chunk, 2 = at most one block per resident slot, on
+// units of 'chunk' planes that a band launch keeps); order 2 in 3D has rows
+// of SEG3D_O2 output columns.
 inline void plan_cartesian(GridParams &gp, int chunk, int by = 16, int wpb = 0, int tile3d = 0, int order = 1)
 {
     const int seg = (gp.dim == 3 && order == 2) ? SEG3D_O2 : SEG;
     gp.nseg = (gp.n[0] + seg - 1) / seg;
     gp.wpb = (wpb >= 1 && wpb <= WARPS_2D) ? wpb : WARPS_2D;
-    gp.tile3d = (gp.dim == 3 && tile3d) ? 1 : 0;
+    gp.tile3d = (gp.dim == 3 && tile3d >= 1 && tile3d <= 2) ? tile3d : 0;
     gp.chunk0 = 0;
     gp.bookkeep = 1;
+    gp.unit = chunk > 0 ? chunk : 32;
     if (gp.dim == 2) {
         gp.chunk = chunk > 0 ? chunk : 32;
         gp.nchunk = (gp.n[1] + gp.chunk - 1) / gp.chunk;
@@ -53,10 +58,40 @@ inline long long cartesian_blocks(const GridParams &gp)
     return (long long)gp.nseg * gp.nrowblk * gp.nchunk;
 }
 
+// Blocks of the 3D tile kernel that are resident at once on the current
+// device (SMs x blocks per SM), found once per kernel.
+template <class A, int STAGE>
+inline long long tile3d_slots()
+{
+    static const long long slots = [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage3d_tile_kernel<A, STAGE>, TILE_X * TILE_Y,
+                                                          0) != cudaSuccess) {
+            cudaGetLastError();
+            return 152LL;
+        }
+        return (long long)std::max(sms, 1) * std::max(per_sm, 1);
+    }();
+    return slots;
+}
+
 template <class A, int STAGE, bool HAS3D>
 inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cudaStream_t s)
 {
-    const unsigned blocks = (unsigned)cartesian_blocks(gp);
+    long long nb = cartesian_blocks(gp);
+    if constexpr (HAS3D) {
+        // at most one block per slot, and at least a plane per block
+        if (gp.dim == 3 && gp.tile3d == 2) {
+            const long long zlo = (long long)gp.chunk0 * gp.chunk;
+            const long long nzr = std::min<long long>(gp.n[2], zlo + (long long)gp.nchunk * gp.chunk) - zlo;
+            const long long ntiles =
+                (long long)((gp.n[0] + TILE_X - 1) / TILE_X) * ((gp.n[1] + TILE_Y - 1) / TILE_Y);
+            nb = std::min(ntiles * nzr, tile3d_slots<A, STAGE>());
+        }
+    }
+    const unsigned blocks = (unsigned)nb;
     if (gp.dim == 2) {
         stage2d_kernel<A, STAGE><<<blocks, gp.wpb * 32, 0, s>>>(gp, sa);
     } else {

@@ -196,7 +196,8 @@ class CartesianEuler:
 
     def set_shape(self, chunk, variant):
         """Pin the decomposition: rows / planes per chunk, and warps per block
-        (2D) or the 3D kernel (0 = row blocks, 1 = tiles)."""
+        (2D) or the 3D kernel (0 = row blocks, 1 = tiles with one block per
+        tile and chunk, 2 = tiles with one block per resident slot)."""
         capi.check(self._lib.mmf_set_shape(self._ctx, chunk, variant))
 
     def autotune(self, trial_steps=4):

@@ -143,12 +143,13 @@ def test_compute_rhs_ragged_bitwise(orc, mmf, dim, n, periodic):
 
 @pytest.mark.parametrize("arith", ["reference", "fast"])
 @pytest.mark.parametrize("n,periodic", [((61, 14, 9), False), ((40, 35, 11), True), ((32, 16, 8), True),
-                                        ((1, 17, 5), False)])
+                                        ((1, 17, 5), False), ((70, 50, 23), True)])
 def test_3d_kernels_give_the_same_bits(orc, mmf, arith, n, periodic):
     """The two 3D order-1 kernels -- row blocks of 30-column segments with
-    halo lanes and rows, and 32 x 16 tiles with one-pass halo records -- and
-    every plane chunk give the same bits, on grids that the tiles divide and
-    on ragged ones; with the reference arithmetic they are the oracle's."""
+    halo lanes and rows, and 32 x 16 tiles with one-pass halo records, one
+    block per tile and chunk or at most one per resident slot -- and every
+    plane chunk give the same bits, on grids that the tiles divide and on
+    ragged ones; with the reference arithmetic they are the oracle's."""
     P = mmf.problem
     case = P.Case("ragged3d", P.RADSOD, 3, n, (-0.3, -0.2, -0.1), 1.0, 0.5, periodic=periodic,
                   prm=P.Params(sod_radius=0.3))
@@ -157,7 +158,11 @@ def test_3d_kernels_give_the_same_bits(orc, mmf, arith, n, periodic):
     U0 = m.initial_state(oracle_params(orc, case)) * (1.0 + 0.05 * rng.standard_normal((m.ncells, 1)))
     steps = 6
     outs = []
-    for variant, chunk in [(0, 4), (1, 4), (1, 3), (1, 64)]:
+    # variant 2 on the 70 x 50 x 23 grid: 12 tile columns x 23 planes on at
+    # most one block per slot; 4-plane units all fall in the evenly split
+    # last round (shares that start and end inside columns), 1-plane units
+    # make one whole round and a partial one
+    for variant, chunk in [(0, 4), (1, 4), (1, 3), (1, 64), (2, 4), (2, 1)]:
         with case.solver(arith=arith) as s:
             s.set_shape(chunk, variant)
             U, t, done = s.run(U0, case.cfl, max_steps=steps)
