@@ -624,6 +624,10 @@ int mmf_time_setup(mmf_ctx *c, double cfl, double t, double t_end, int64_t max_s
 static int build_graph(mmf_ctx *c, int steps, cudaGraphExec_t *exec)
 {
     cudaGraph_t g = nullptr;
+    if (c->gp.dim == 3 && c->gp.tile3d == 2) {
+        if (c->grid.arith == MMF_ARITH_REFERENCE) prime_tile3d_exact();
+        else prime_tile3d_fast();
+    }
     MMF_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t err = cudaSuccess;
     const long long before = c->launches;

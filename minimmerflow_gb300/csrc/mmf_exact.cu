@@ -12,6 +12,8 @@ cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs 
     return launch_stage<ExactArith>(stage, gp, sa, s);
 }
 
+void prime_tile3d_exact() { prime_tile3d_slots<ExactArith>(); }
+
 cudaError_t launch_screen_selftest_exact(int dim, long long n, const double *uc, const double *sig, int *dec,
                                         unsigned char *ref, cudaStream_t s)
 {

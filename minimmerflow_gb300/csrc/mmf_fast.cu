@@ -15,6 +15,8 @@ cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &
     return launch_stage<FastArith>(stage, gp, sa, s);
 }
 
+void prime_tile3d_fast() { prime_tile3d_slots<FastArith>(); }
+
 cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageArgs &sa, const O2Args &oa,
                            double *W1, cudaStream_t s, bool w_zero)
 {

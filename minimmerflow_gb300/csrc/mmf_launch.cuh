@@ -77,6 +77,17 @@ inline long long tile3d_slots()
     return slots;
 }
 
+// The slot counts of the four stage instantiations, found before a stream
+// capture so that no occupancy query runs inside one.
+template <class A>
+inline void prime_tile3d_slots()
+{
+    tile3d_slots<A, STAGE_RHS>();
+    tile3d_slots<A, STAGE_1>();
+    tile3d_slots<A, STAGE_2>();
+    tile3d_slots<A, STAGE_3>();
+}
+
 template <class A, int STAGE, bool HAS3D>
 inline cudaError_t launch_stage_t(const GridParams &gp, const StageArgs &sa, cudaStream_t s)
 {
@@ -177,6 +188,8 @@ cudaError_t launch_o2_fast(int op, int stage, const GridParams &gp, const StageA
 // 2D kernels that skip the identically-zero z-momentum.
 cudaError_t launch_stage_exact(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s);
 cudaError_t launch_stage_fast(int stage, const GridParams &gp, const StageArgs &sa, cudaStream_t s, bool w_zero);
+void prime_tile3d_exact();
+void prime_tile3d_fast();
 
 // Self-test of the FP32 positivity screen of the order-2 slopes (nv 4: the 2D
 // four-field layout of the fast arithmetic).
