@@ -1190,9 +1190,9 @@ def main():
     traffic = None
     tkey = ("3d_%d" if r["case"].dim == 3 else "%d") % args.n
     if r["case"].dim == 3:
-        # the captured 3D decompositions: tiles with one block per tile and
-        # 32-plane chunk, and on one block per resident slot with 128-plane units
-        tkey = {(-1, 32): tkey, (-2, 128): tkey + "_slots"}.get((r["tuned"][1], r["tuned"][0]))
+        # the captured 3D decomposition: tiles on one block per resident slot
+        # with 128-plane units
+        tkey = {(-2, 128): tkey + "_slots"}.get((r["tuned"][1], r["tuned"][0]))
     if args.order == 1 and traffic_rec and tkey in traffic_rec.get("per_launch_bytes", {}):
         traffic = traffic_rec["per_launch_bytes"][tkey].get("stage%d" % dom)
     fp64_ops = fp64_ops_per_cell_update_2d() if (args.workload == "sod2d" and args.order == 1) else None
@@ -1262,11 +1262,10 @@ def main():
                               warmup=w_extra, clocks=True)
                 d3 = r3["dominant"]
                 ach3 = STAGE_BYTES[d3] * r3["ncell"] / r3["st_mean"][d3] / 1e9
-                # ncu DRAM bytes of the captured decompositions: the tile kernel
-                # with one block per tile and 32-plane chunk, or on one block per
-                # resident slot with 128-plane units
+                # ncu DRAM bytes of the captured decomposition: the tile kernel on
+                # one block per resident slot with 128-plane units
                 tr3 = read_traffic() or {}
-                tkey3 = {(-1, 32): "3d_256", (-2, 128): "3d_256_slots"}.get((r3["tuned"][1], r3["tuned"][0]))
+                tkey3 = {(-2, 128): "3d_256_slots"}.get((r3["tuned"][1], r3["tuned"][0]))
                 traffic3 = tr3.get("per_launch_bytes", {}).get(tkey3, {}).get("stage%d" % d3) if tkey3 else None
                 v3["axis_" + wl[-1]] = {"value": r3["value"], "unit": metric, "cells": r3["ncell"],
                                         "steps": max(k_extra, 20), "step_times": step_stats(r3["durs"]),

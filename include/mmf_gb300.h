@@ -135,7 +135,7 @@ void *mmf_get_stream(mmf_ctx *ctx);
 /* Chooses the work decomposition of the stage kernels by timing a few steps
  * of each candidate from the current state (2D: rows per marching chunk x
  * warps per block; 3D: planes per chunk x, at order 1, the 3D kernel: row
- * blocks or 32 x 16 tiles, the tiles with one block per tile and chunk or
+ * blocks or 32 x 8 tiles, the tiles with one block per tile and chunk or
  * one block per resident slot); restores the state and the time control
  * afterwards.  Results are bitwise independent of the choice.  Needs
  * mmf_time_setup.  warps_per_block receives the warps per block in 2D, and
@@ -145,11 +145,11 @@ void *mmf_get_stream(mmf_ctx *ctx);
 int mmf_autotune(mmf_ctx *ctx, int trial_steps, int *chunk, int *warps_per_block);
 /* Sets the work decomposition directly: rows (2D) or planes (3D) per
  * marching chunk, and 'variant' = warps per block in 2D (1..4), the 3D
- * kernel in 3D (0 = row blocks; 1 = 32 x 16 tiles, one block per tile and
- * chunk; 2 = 32 x 16 tiles, as many blocks up to one per resident slot,
- * each marching an even share of the tile columns' planes, the default; 1
- * and 2 are order 1 only).  Results are bitwise independent of the choice.  No reference
- * counterpart. */
+ * kernel in 3D (0 = row blocks; 1 = 32 x 8 tiles, one block per tile and
+ * chunk; 2 = 32 x 8 tiles on at most one block per resident slot (two per
+ * SM): whole rounds of (tile column, 'chunk'-plane) units, the last round
+ * split evenly by planes; the default; 1 and 2 are order 1 only).  Results
+ * are bitwise independent of the choice.  No reference counterpart. */
 int mmf_set_shape(mmf_ctx *ctx, int chunk, int variant);
 /* Per-step log, the values the reference prints each step (src/main.cpp:
  * 399-404): maxEig, the dt used and the time after the step.  The device

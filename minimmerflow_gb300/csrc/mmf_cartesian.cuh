@@ -59,7 +59,7 @@ struct GridParams {
     int chunk0;     // first chunk of the launch (a launch may cover a band of the grid)
     int bookkeep;   // this launch updates the control block (exactly one launch per stage)
     int wpb;        // 2D: warps per block
-    int tile3d;     // 3D order 1: 0 = row-block kernel, 1 = 32 x 16 tile kernel with one block per tile and
+    int tile3d;     // 3D order 1: 0 = row-block kernel, 1 = 32 x 8 tile kernel with one block per tile and
                     // chunk, 2 = the tile kernel on at most one block per resident slot
     int unit;       // tile3d 2: planes per (column, unit) work unit (a band launch keeps the whole grid's)
     long long plane;  // cells per field plane
@@ -516,9 +516,12 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
 }
 
 // ---------------------------------------------------------- 3D tile kernel
-// Block = 16 warps over a tile of 32 x 16 cells (x = lane, y = warp) that
-// marches along z.  Every lane and warp owns an output cell, so tiles divide
-// 256-cell grid lines exactly.  The records the tile's faces need from the
+// Block = 8 warps over a tile of 32 x 8 cells (x = lane, y = warp) that
+// marches along z, two blocks per SM (128 registers a thread), so that one
+// block computes while the other waits at a barrier; one block of 16 warps
+// over 32 x 16 cells per SM, with half the halo records per cell, ran the
+// 256^3 vortex 3% slower.  Every lane and warp owns an output cell, so tiles
+// divide 256-cell grid lines exactly.  The records the tile's faces need from the
 // four neighbouring lines (the column left and right of the tile, the row
 // below and above it) are evaluated once per plane by three warps in one
 // extra pass each (x or y part only), and the faces on the tile's left,
@@ -534,13 +537,15 @@ __global__ void __launch_bounds__(BY * 32) stage3d_kernel(GridParams gp, StageAr
 // different SM sub-partitions (warp w runs on sub-partition w % 4): the halo
 // records on 1, 2 and 3 (between (B) and (A)), the edge faces on 0 and 3
 // (between (A) and (B)).
-constexpr int TILE_X = 32, TILE_Y = 16;
+constexpr int TILE_X = 32, TILE_Y = 8;
+static_assert(TILE_Y == 8 || TILE_Y == 16, "tile rows: 8 (two blocks per SM) or 16 (one)");
+constexpr int TILE_MIN_BLOCKS = TILE_Y == 8 ? 2 : 1;   // blocks per SM the register cap is for
 constexpr int TW_TOP = 5, TW_BOT = 6, TW_SIDE = 7;   // warps of the halo-record passes
 constexpr int TW_BOTF = 4, TW_LEFTF = 3;             // warps of the edge-face passes
 
 template <int NV>
 struct SmemTile {
-    double yc[TILE_Y + 1][NV][32];   // y-face side (state, y flux, y speed) of rows 0..15 and the top halo row
+    double yc[TILE_Y + 1][NV][32];   // y-face side (state, y flux, y speed) of the rows and the top halo row
     double yf[TILE_Y + 1][NV][32];
     double ylam[TILE_Y + 1][32];
     double bc[NV][32], bf[NV][32], blam[32];                        // bottom halo row
@@ -572,8 +577,8 @@ __device__ __forceinline__ void tile_halo_records(const StageArgs &sa, const Gri
             for (int k = 0; k < NV; ++k) { sm.bc[k][l] = h.c[k]; sm.bf[k][l] = h.f[1][k]; }
             sm.blam[l] = h.lam[1];
         }
-    } else if (w == TW_SIDE) {
-        const int side = l >> 4, r = l & 15;
+    } else if (w == TW_SIDE && l < 2 * TILE_Y) {
+        const int side = l / TILE_Y, r = l % TILE_Y;
         RecOf<A, 3> h;
         load_record<A, STAGE, 3>(sa, gp, sc, side ? x0 + TILE_X : x0 - 1, y0 + r, z, h, nullptr);
 #pragma unroll
@@ -601,7 +606,7 @@ __device__ __forceinline__ void tile_publish(SmemTile<NV> &sm, const CellRecV<3,
 }
 
 template <class A, int STAGE>
-__global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParams gp, StageArgs sa)
+__global__ void __launch_bounds__(TILE_X * TILE_Y, TILE_MIN_BLOCKS) stage3d_tile_kernel(GridParams gp, StageArgs sa)
 {
     constexpr int NV = A::NVAR;
     __shared__ SmemTile<NV> sm;
@@ -697,11 +702,11 @@ __global__ void __launch_bounds__(TILE_X * TILE_Y) stage3d_tile_kernel(GridParam
 #pragma unroll
                 for (int k = 0; k < NV; ++k) sm.Fy[w][k][l] = Fyt[k];
             }
-            // faces on the tile's left edge (lanes 0..15: rows), right edge (lanes
-            // 16..31: rows) and bottom edge (lanes: columns)
-            if (w == TW_LEFTF) {
-                const int r = l & 15;
-                const bool right = l >= 16;
+            // faces on the tile's left edge (lanes 0..TILE_Y-1: rows), right
+            // edge (the next TILE_Y lanes: rows) and bottom edge (lanes: columns)
+            if (w == TW_LEFTF && l < 2 * TILE_Y) {
+                const int r = l % TILE_Y;
+                const bool right = l >= TILE_Y;
                 double cL[NV], fL[NV], cR[NV], fR[NV], F[NV];
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
