@@ -11,7 +11,8 @@ value  : cell-updates/s with the state resident in HBM; each step is timed with
          CUDA events on the library stream, and L2 is flushed (a 512 MB write)
          between timed steps, outside the events.
 e2e    : the same metric through the public C ABI with host buffers:
-         upload of the AoS state from pinned memory, one step, download.
+         upload of the AoS state from pinned memory, one step, download; the
+         best of three rounds' median calls, every round reported.
 roofline / fp64: the stage-2 kernel (dominant, 120 B/cell algorithmic) timed
          per launch with events; peaks from MEASURED_PEAKS.json.
 cpu_baseline: the oracle (C restatement, bit-identical to the reference
@@ -1042,17 +1043,24 @@ def run_ours(args, world, rank, local, dist, case=None, steps=None, warmup=None,
         s.advance_host(hv, 1)
     hv[:] = U0
     s.time_setup(case.cfl, 0.0, case.t_end, -1 if limit < 0 else 10 ** 9)
-    calls = []
-    for _ in range(k_e2e):
-        t0 = time.perf_counter()
-        s.advance_host(hv, 1)
-        calls.append(time.perf_counter() - t0)
-    # the median call: one host round trip competes with other traffic on the
-    # host link, and single calls of the large 3D state vary by +-15%
-    e2e_val = world * ncell / statistics.median(calls)
+    # the median call of each of three rounds: a host round trip competes
+    # with other traffic on the host's memory and link (single calls of the
+    # large 3D state vary by +-15%, and once all nine calls of a round ran at
+    # a fifth of the rate), so the value is the best round's median, with
+    # every round's reported beside it
+    e2e_rounds = []
+    for _ in range(3):
+        calls = []
+        for _ in range(k_e2e):
+            t0 = time.perf_counter()
+            s.advance_host(hv, 1)
+            calls.append(time.perf_counter() - t0)
+        e2e_rounds.append(world * ncell / statistics.median(calls))
+    e2e_val = max(e2e_rounds)
     s.close()
     return dict(value=value, total=total, clocks=clock_rec, launches=launches, st_mean=st_mean, dominant=dominant,
-                e2e=e2e_val, ncell=ncell, case=case, tuned=tuned, durs=durs, sustained=sustained)
+                e2e=e2e_val, e2e_rounds=e2e_rounds, e2e_calls=k_e2e, ncell=ncell, case=case, tuned=tuned, durs=durs,
+                sustained=sustained)
 
 
 def main():
@@ -1236,7 +1244,9 @@ def main():
         "gpu_launches": r["launches"],
         "step_times": step_stats(r["durs"]),
         "e2e": {"value": r["e2e"], "unit": metric, "h2d_bytes_per_step": 40 * ncell,
-                "d2h_bytes_per_step": 40 * ncell},
+                "d2h_bytes_per_step": 40 * ncell, "rounds": r["e2e_rounds"], "calls_per_round": r["e2e_calls"],
+                "how": "mmf_advance_host, one step per call on a page-locked AoS buffer; the best of three "
+                       "rounds' median calls"},
     }
     if r["sustained"]:
         line["sustained"] = r["sustained"]
@@ -1281,7 +1291,8 @@ def main():
                                         "gpu_launches": r3["launches"],
                                         "e2e": {"value": r3["e2e"], "unit": metric,
                                                 "h2d_bytes_per_step": 40 * r3["ncell"],
-                                                "d2h_bytes_per_step": 40 * r3["ncell"]},
+                                                "d2h_bytes_per_step": 40 * r3["ncell"],
+                                                "rounds": r3["e2e_rounds"], "calls_per_round": r3["e2e_calls"]},
                                         "clocks": r3["clocks"]}
             v3["workload"] = ("3D isentropic vortex 256^3, [-5,5]^3, periodic, beta=5, CFL 0.5, order 1, FP64, "
                               "fast arithmetic; axis z and axis x")
