@@ -365,6 +365,29 @@ def test_full_size_vortex3d_is_invariant_along_its_axis(mmf, axis):
         assert rel_err(planes[0].reshape(-1, 5), U2) <= FAST_RTOL
 
 
+def test_full_size_3d_decompositions_agree(mmf):
+    """At the benchmark's 256^3, the row-block kernel, the tile kernel with
+    one block per tile and 32-plane chunk, and the tile kernel on one block
+    per resident slot (128-plane units: a whole round and an evenly split
+    last one; 8-plane units: many rounds) give the same bits over five steps
+    of a seeded, perturbed radial Sod, which has no symmetry that would hide
+    a misplaced plane, row or column."""
+    P = mmf.problem
+    case = P.radial_sod_ratios(256, 10.0, 4.0, dim=3)
+    rng = np.random.default_rng(11)
+    U0 = case.initial_state() * (1.0 + 0.01 * rng.standard_normal((256 ** 3, 1)))
+    outs = []
+    for chunk, variant in [(32, 0), (32, 1), (128, 2), (8, 2)]:
+        with case.solver(arith="fast") as s:
+            s.set_shape(chunk, variant)
+            U, t, steps = s.run(U0, case.cfl, max_steps=5)
+            assert steps == 5 and s.status() == 0
+        outs.append((U, t))
+    for U, t in outs[1:]:
+        assert t == outs[0][1]
+        assert np.array_equal(U, outs[0][0])
+
+
 def test_advance_stops_at_the_end_time(mmf):
     """mmf_advance with many more steps than the run needs launches no idle
     graphs: it returns promptly once t_end is reached."""
