@@ -45,7 +45,7 @@ struct mmf_ctx {
     unsigned char *ind_raw = nullptr;   // the network's flags before the dilation (period 2)
     // pipelined host round trip (mmf_advance_host): a copy stream, one event
     // per band and direction, pinned host words for the flag and the control block
-    static constexpr int MAX_BANDS = 8;
+    static constexpr int MAX_BANDS = 16;
     cudaStream_t copy_stream = nullptr;
     cudaStream_t tr_stream = nullptr;            // upload transpositions, highest priority
     cudaStream_t band_stream[MAX_BANDS] = {};   // band b at priority b (band 0 first)
