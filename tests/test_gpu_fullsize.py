@@ -4,7 +4,8 @@ full meshes the benchmark measures, not on reduced copies of them.
 - 2D radial Sod, 1024^2 cells on [-1,1]^2, rho = p = 1 for r < 0.5 and
   rho = 0.125, p = 0.1 outside, zero velocity, transmissive borders, CFL 0.5:
   the first 128 steps of the run to t = 0.25 (the reference loop,
-  src/main.cpp:377-506, restated by the oracle; about 35 s of oracle time).
+  src/main.cpp:377-506, restated by the oracle; about 35 s of oracle time),
+  on the Cartesian kernels and on the face-list kernels.
 - 3D periodic isentropic vortex, beta = 5, on [-5,5]^3 at 64^3, 50 steps,
   vortex axis along z and along x.
 - Order 2 (MC limiter on every cell): the 1024^2 radial Sod at CFL 0.4, 10
@@ -63,6 +64,20 @@ def test_full_size_sod_1024_matches_oracle(orc, mmf, arith):
     else:
         assert abs(t - t_ref) <= 1e-13 * t_ref
         assert rel_err(U, U_ref) <= FAST_RTOL
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_full_size_sod_1024_face_lists_match_oracle(orc, mmf, arith):
+    """The face-list solver (the path for meshes that are not one lattice) on
+    the same 1024^2 Sod and 128 steps, against the same oracle run."""
+    from minimmerflow_gb300.umesh import UnstructuredEuler
+    case = mmf.problem.radial_sod_2d(n=1024)
+    U0, U_ref, t_ref = _oracle_run(orc, case, SOD_STEPS)
+    m = oracle_mesh(orc, case)
+    with UnstructuredEuler.from_oracle_mesh(m, arith=arith) as u:
+        U, t, steps = u.run(U0, case.cfl, max_steps=SOD_STEPS)
+    assert steps == SOD_STEPS
+    _check(U, t, U_ref, t_ref, arith)
 
 
 @pytest.mark.parametrize("arith", ["reference", "fast"])
